@@ -1,0 +1,348 @@
+"""Benchmark of the RTM propagate/migrate path on one GB300 (or N, one
+process per GPU, shots sharded across ranks).
+
+Workload (default): the plain multi-shot configuration -- a 401x1201 seeded
+layered model (12 dipping layers 1500-5500 m/s, two normal faults, a
+low-velocity lens), dx=dz=12.5 m, dt=1 ms, 4000 steps, M=8 adaptive
+least-squares coefficients, 30-cell hybrid ABC, 64 surface shots with
+full-spread receivers, images stacked with Kahan summation.  A step is the
+full migration of the 64 shots: forward source run, boundary-ring
+reconstruction, receiver back-propagation, imaging, per-shot finishing and
+the stack.  The observed gathers are modelled first (true model minus
+smoothed model, removing the direct wave) and stay resident in HBM for
+`value`; `e2e` takes them from pinned host memory every step and returns the
+image to the host.
+
+Metric: grid-cell updates per second, one update = one grid point advanced
+one time step; per shot NT*(2*NZ*NX + nz*nx) (forward on the padded grid,
+receiver wavefield on the padded grid, source reconstruction on the interior).
+
+--impl reference times the reference's own propagation + imaging loop
+(kernel.cu kernel bodies, compiled for the host cores by oracle/build_ref.py)
+on a bounded sample of the same workload, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s"
+
+
+def cell_updates_per_shot(nz, nx, N2, NT):
+    NZ, NX = nz + 2 * N2, nx + 2 * N2
+    return NT * (2 * NZ * NX + nz * nx)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--nt", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=0, help="shots per batch (0: all)")
+    ap.add_argument("--coef", default="adaptive", choices=["adaptive", "taylor"])
+    ap.add_argument("--cpu-sample-nt", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
+    return ap.parse_args()
+
+
+class Config:
+    def __init__(self, a):
+        self.small = a.small
+        self.nz, self.nx = (101, 301) if a.small else (401, 1201)
+        self.N2, self.M = 30, 8
+        self.h, self.tao, self.f0 = 12.5, 0.001, 25.0
+        self.NT = a.nt
+        self.nshot = a.shots
+        self.coef = a.coef
+        self.whitecoe = 1e-4
+        # optimiser settings (the reference's parameter file: nthita=1000,
+        # eps=1e-5, df=1; fmax = 2*f0)
+        self.fmax, self.df, self.nthita, self.eps, self.nfdmin = 2 * self.f0, 1.0, 1000, 1e-5, 2
+
+    def workload(self):
+        return {"workload": "multi-shot FP32 RTM %dx%d interior, 30-cell hybrid ABC, M=%d %s, "
+                            "%d steps, %d surface shots, full-spread receivers, Kahan stack"
+                            % (self.nz, self.nx, self.M, self.coef, self.NT, self.nshot),
+                "nz": self.nz, "nx": self.nx, "N2": self.N2, "M": self.M, "nt": self.NT,
+                "shots": self.nshot, "dx_m": self.h, "dt_s": self.tao, "coefficients": self.coef}
+
+
+def build_problems(cfg, dv=1.0):
+    from rtm_gpu_gb300 import synth
+    from rtm_gpu_gb300.problem import build_problem
+    vtrue = synth.model_c2(nz=cfg.nz, nx=cfg.nx)
+    vmig = synth.smooth_model(vtrue, 10.0)
+    rec = synth.full_spread(cfg.nx, cfg.N2)
+    table = None
+    if cfg.coef == "adaptive":
+        from rtm_gpu_gb300 import coeffs
+        table = coeffs.table_source(nfdmax=cfg.M, nfdmin=cfg.nfdmin, tao=cfg.tao, h=cfg.h,
+                                    fmax=cfg.fmax, df=cfg.df, nthita=cfg.nthita, eps=cfg.eps)
+    kw = dict(N2=cfg.N2, M=cfg.M, NT=cfg.NT, h=cfg.h, tao=cfg.tao, f0=cfg.f0,
+              adaptive=cfg.coef == "adaptive", compen=True, rec=rec, dv=dv, coef_table=table)
+    ptrue = build_problem(vtrue, **kw)
+    pmig = build_problem(vmig, **kw)
+    shots = synth.surface_shots(cfg.nx, cfg.nshot, cfg.N2)
+    return ptrue, pmig, shots
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self, dev_index=0):
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9 and r[0].strip() == str(dev_index)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(cfg, pmig, shots, seis_host, nt_sample, threads):
+    """Reference kernel bodies (oracle/_ref) or, failing that, the oracle's
+    C restatement, timed on the host cores on one shot with nt_sample steps."""
+    import dataclasses
+    from oracle import oracle as orc
+    kind = "reference"
+    try:
+        orc.ref()
+    except Exception:
+        kind = "port"
+    orc.set_threads(threads)
+    p = dataclasses.replace(pmig, NT=nt_sample, wav=pmig.wav[: nt_sample + 1])
+    p = p.with_source(*shots[0])
+    s = np.ascontiguousarray(seis_host[0][:, :nt_sample])
+    t0 = time.perf_counter()
+    orc.migrate(p, s, use_ref=(kind == "reference"))
+    dt = time.perf_counter() - t0
+    cu = cell_updates_per_shot(p.nz, p.nx, p.N2, nt_sample)
+    return {"value": cu / dt / 1e9, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": "one shot of the workload grid, %d time steps (%.3g cell-updates), %.1f s"
+                      % (nt_sample, cu, dt)}
+
+
+def run_reference_arm(a, cfg):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from rtm_gpu_gb300.problem import build_problem
+    from rtm_gpu_gb300 import synth
+    import dataclasses
+    from oracle import oracle as orc
+    # the reference arm needs no GPU: a Taylor problem of the same grid for
+    # the loop (coefficient count M=8 per cell as the adaptive table at M=8)
+    vmig = synth.smooth_model(synth.model_c2(nz=cfg.nz, nx=cfg.nx), 10.0)
+    nt = a.cpu_sample_nt or (60 if not cfg.small else 200)
+    p = build_problem(vmig, N2=cfg.N2, M=cfg.M, NT=nt, h=cfg.h, tao=cfg.tao, f0=cfg.f0,
+                      adaptive=False, compen=True, rec=synth.full_spread(cfg.nx, cfg.N2))
+    shots = synth.surface_shots(cfg.nx, cfg.nshot, cfg.N2)
+    rng = np.random.default_rng(7)
+    seis = (rng.standard_normal((1, p.nrec, nt)) * 1e-3).astype(np.float32)
+    threads = os.cpu_count() or 1
+    for _ in range(a.warmup):
+        cpu_baseline(cfg, p, shots, seis, nt, threads)
+    vals = [cpu_baseline(cfg, p, shots, seis, nt, threads) for _ in range(a.steps)]
+    v = float(np.median([x["value"] for x in vals]))
+    cu = cell_updates_per_shot(cfg.nz, cfg.nx, cfg.N2, cfg.NT) * cfg.nshot
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": cu / (v * 1e9) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg.workload(),
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": vals[0]["kind"],
+                             "sample": vals[0]["sample"] + "; ms_per_step extrapolated to the full workload"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    cfg = Config(a)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if a.impl == "reference":
+        run_reference_arm(a, cfg)
+        return
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from rtm_gpu_gb300 import Engine
+    warm = max(3, a.warmup)
+
+    ptrue, pmig, shots = build_problems(cfg)
+    nshot = cfg.nshot
+    batch = a.batch or nshot
+    src = [pmig.src_flat(z, x) for z, x in shots]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    # observed data: true minus smoothed model (direct wave removed)
+    seis = torch.zeros((nshot, pmig.nrec, pmig.NT), dtype=torch.float32, device="cuda")
+    tmp = torch.zeros_like(seis)
+    with Engine(ptrue, batch=batch, stream=sh) as e:
+        e.model(src, out=seis)
+    with Engine(pmig, batch=batch, stream=sh) as e:
+        e.model(src, out=tmp)
+    seis -= tmp
+    del tmp
+    torch.cuda.synchronize()
+
+    eng = Engine(pmig, batch=batch, stream=sh)
+    img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
+    ill = torch.zeros_like(img)
+
+    def step_dev():
+        eng.migrate_stack(src, seis, cfg.whitecoe, nshot, True, image=img, illum=ill)
+
+    for _ in range(warm):
+        step_dev()
+    torch.cuda.synchronize()
+    eng.launches(reset=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+                if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/bench_clocks.csv") as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(a.steps):
+            step_dev()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    launches = eng.launches() // a.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cu_step = cell_updates_per_shot(pmig.nz, pmig.nx, pmig.N2, pmig.NT) * nshot
+    value = cu_step * world / (ms / 1e3) / 1e9
+
+    # end to end through the public API with host buffers
+    seis_h = seis.cpu().pin_memory()
+    img_h = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32).pin_memory()
+    ill_h = torch.zeros_like(img_h).pin_memory()
+    eng.migrate_stack(src, seis_h, cfg.whitecoe, nshot, True, image=img_h, illum=ill_h)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        eng.migrate_stack(src, seis_h, cfg.whitecoe, nshot, True, image=img_h, illum=ill_h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / a.steps
+    if dist:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e = {"value": cu_step * world / (ms_e2e / 1e3) / 1e9, "unit": METRIC,
+           "h2d_bytes_per_step": int(seis_h.numel() * 4),
+           "d2h_bytes_per_step": int((img_h.numel() + ill_h.numel()) * 4)}
+
+    # roofline of the dominant kernel (backward stencil) from a timed pass
+    nb = min(batch, nshot)
+    eng.set_timing(True)
+    r1d = torch.zeros((nb, pmig.NZ, pmig.NX), dtype=torch.float32, device="cuda")
+    eng.migrate(src[:nb], seis[:nb], rel1=r1d, rel2=torch.zeros_like(r1d))
+    del r1d
+    tm = eng.timing()
+    eng.set_timing(False)
+    NZ, NX, nz, nx = pmig.NZ, pmig.NX, pmig.nz, pmig.nx
+    bwd_bytes = nb * (16 * (NZ * NX + nz * nx) + 32 * nz * nx)
+    fwd_bytes = nb * 16 * NZ * NX
+    bwd_ms = tm["bwd_ms"] / max(tm["bwd_n"], 1)
+    fwd_ms = tm["fwd_ms"] / max(tm["fwd_n"], 1)
+    peak, peak_kind = measured_peak()
+    achieved = bwd_bytes / (bwd_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "kernel": "k_step<backward> (source reconstruction + receiver step + imaging)",
+                "bytes_per_launch": bwd_bytes, "launch_ms": bwd_ms, "peak_kind": peak_kind,
+                "forward_kernel": {"launch_ms": fwd_ms, "bytes_per_launch": fwd_bytes,
+                                   "achieved": fwd_bytes / (fwd_ms / 1e3) / 1e9},
+                "pad_kernel_ms": tm["pad_ms"] / max(tm["pad_n"], 1),
+                "time_share": {"fwd": tm["fwd_ms"], "bwd": tm["bwd_ms"], "pad": tm["pad_ms"]}}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        nt_s = a.cpu_sample_nt or 60
+        cpu = cpu_baseline(cfg, pmig, shots, seis_h.numpy(), nt_s, os.cpu_count() or 1)
+
+    clocks = clk.summary(local)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+                "steps": a.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": dict(cfg.workload(), batch=batch,
+                               l2="inputs larger than L2 (%.1f GB of wavefields and rings)"
+                                  % (eng.device_bytes / 1e9)),
+                "shots_per_hour": nshot * world / (ms / 1e3) * 3600,
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": launches}
+        print(json.dumps(line))
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

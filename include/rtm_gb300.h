@@ -1,0 +1,212 @@
+/*
+ * rtm_gb300.h -- C ABI of the GB300 (sm_103a) engine for the 2-D acoustic
+ * reverse-time-migration path of caixh90/RTM_GPU.
+ *
+ * Two levels:
+ *
+ *  1. Kernel level (rtm_k_*): one entry point per __global__ kernel of the
+ *     reference's kernel.cu, with the same argument list, units and
+ *     [iz*NX + ix] row-major layout, plus a trailing stream.  A copy of the
+ *     reference's main() whose "Name<<<gridDim,blockDim>>>(" launches are
+ *     rewritten to "rtm_k_Name(" runs unchanged in logic on these kernels.
+ *     Buffers are caller-owned device pointers; nothing is allocated.
+ *
+ *  2. Shot level (rtm_ctx_*, rtm_model_*, rtm_migrate_*, ...): a context owns
+ *     the device copies of the model and the per-shot wavefields, and advances
+ *     a batch of shots together through fused, TMA-staged kernels (captured in
+ *     CUDA graphs).  Host buffers are caller-owned; device buffers are
+ *     context-owned.  A context is thread-compatible (not thread-safe).
+ *
+ * Every function returns RTM_OK (0) or a negative status; rtm_last_error()
+ * gives a message for the calling thread's last failure.
+ */
+#ifndef RTM_GB300_H
+#define RTM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *rtm_stream_t; /* a cudaStream_t; NULL = legacy default stream */
+
+enum {
+    RTM_OK = 0,
+    RTM_ERR_ARG = -1,       /* invalid argument or size                         */
+    RTM_ERR_CUDA = -2,      /* CUDA runtime error (message in rtm_last_error)   */
+    RTM_ERR_NOMEM = -3,     /* device or host allocation failed                 */
+    RTM_ERR_DEVICE = -4,    /* a kernel reported a device-side error            */
+    RTM_ERR_UNSUPPORTED = -5
+};
+
+const char *rtm_last_error(void);
+int rtm_version(void);
+/* Device-side error word (bit 0: a bounded TMA wait gave up); cleared on read. */
+int rtm_device_error(unsigned int *code);
+
+/* ======================================================================
+ * 1. Kernel level: drop-in replacements for kernel.cu's kernels.
+ *    Each cites the reference kernel it replaces.
+ * ====================================================================== */
+
+/* kernel.cu:18-45 Equal */
+int rtm_k_Equal(float *Dlf, float *Drt, float *Dup, float *Ddw, float *DFW0, float *DFW1, int NZ,
+                int NX, int N2, int nfdmax, rtm_stream_t s);
+/* kernel.cu:46-80 Add */
+int rtm_k_Add(float *Dv, float *DFW2, float *DFW0, float *DFW1, float *Dc, int *DIndex, float tao2,
+              float h2, float vmin, float dv, int nfdmax, int NZ, int NX, int NXZ, int r_u, int r_x,
+              float wavelet, float hzx2_1, rtm_stream_t s);
+/* kernel.cu:82-114 Add_Con */
+int rtm_k_Add_Con(float *Dv, float *DFW2, float *DFW0, float *DFW1, float *Dc, float tao2, float h2,
+                  int nfdmax, int NZ, int NX, int NXZ, int r_u, int r_x, float wavelet,
+                  float hzx2_1, rtm_stream_t s);
+/* kernel.cu:116-158 Hybrid1 */
+int rtm_k_Hybrid1(float *DFW1, float *DFW0, float *DFW2, float *DFWb, float *Dlf, float *Drt,
+                  float *Dup, float *Ddw, float *Dv, float *Dr_1, float *Dw, int NZ, int NX, int N2,
+                  int nfdmax, int k, float taoh, float taoh2, rtm_stream_t s);
+/* kernel.cu:160-183 Hybrid2 */
+int rtm_k_Hybrid2(float *DFW1, float *DFW0, float *DFW2, float *DFWb, float *Dlf, float *Drt,
+                  float *Dup, float *Ddw, float *Dv, float *Dr_1, float *Dw, int NZ, int NX, int N2,
+                  int nfdmax, int k, float taoh, float taoh2, rtm_stream_t s);
+/* kernel.cu:184-208 Hybrid3 */
+int rtm_k_Hybrid3(float *DFW1, float *DFW0, float *DFW2, float *DFWb, float *Dlf, float *Drt,
+                  float *Dup, float *Ddw, float *Dv, float *Dr_1, float *Dw, int NZ, int NX, int N2,
+                  int nfdmax, int k, float taoh, float taoh2, rtm_stream_t s);
+/* kernel.cu:210-221 Deliver */
+int rtm_k_Deliver(float *DFW1, float *DFW0, float *DFW2, int NZ, int NX, rtm_stream_t s);
+/* kernel.cu:222-245 BKEqual */
+int rtm_k_BKEqual(float *Dlf, float *Drt, float *Dup, float *Ddw, float *DFW1, int NZ, int NX,
+                  int N2, int nfdmax, int k, rtm_stream_t s);
+/* kernel.cu:246-283 BKAdd_EFF */
+int rtm_k_BKAdd_EFF(float *Dv, float *DFW2, float *DFW0, float *DFW1, float *Dc, int *DIndex,
+                    float tao2, float h2, float vmin, float dv, int N2, int NZ, int NX, int NXZ,
+                    int r_u, int r_x, float wavelet, float hzx2_1, rtm_stream_t s);
+/* kernel.cu:286-320 BKAdd_EFF_Con */
+int rtm_k_BKAdd_EFF_Con(float *Dv, float *DFW2, float *DFW0, float *DFW1, float *Dc, float tao2,
+                        float h2, int N2, int NZ, int NX, int NXZ, int r_u, int r_x, int nfdmax,
+                        float wavelet, float hzx2_1, rtm_stream_t s);
+/* kernel.cu:323-337 Deliver_EFF */
+int rtm_k_Deliver_EFF(float *DFW1, float *DFW0, float *DFW2, int N2, int NZ, int NX,
+                      rtm_stream_t s);
+/* kernel.cu:339-380 BKAdd */
+int rtm_k_BKAdd(float *Dv, float *DBW2, float *DBW1, float *DBW0, float *Dc, int *DIndex,
+                float *Dseis, float tao2, float h2, float vmin, float dv, int nfdmax, int NZ,
+                int NX, int NXZ, int s_l, int s_r, int s_z, int ds, float hzx2_1, rtm_stream_t s);
+/* kernel.cu:381-418 BKAdd_Con */
+int rtm_k_BKAdd_Con(float *Dv, float *DBW2, float *DBW1, float *DBW0, float *Dc, float *Dseis,
+                    float tao2, float h2, int nfdmax, int NZ, int NX, int NXZ, int s_l, int s_r,
+                    int s_z, int ds, float hzx2_1, rtm_stream_t s);
+/* kernel.cu:421-463 BKHybrid1 */
+int rtm_k_BKHybrid1(float *DFW1, float *DFW0, float *DFW2, float *DFWb, float *Dv, float *Dr_1,
+                    float *Dw, int NZ, int NX, int N2, float taoh, float taoh2, rtm_stream_t s);
+/* kernel.cu:464-487 BKHybrid2 */
+int rtm_k_BKHybrid2(float *DFW1, float *DFW0, float *DFW2, float *DFWb, float *Dv, float *Dr_1,
+                    float *Dw, int NZ, int NX, int N2, float taoh, float taoh2, rtm_stream_t s);
+/* kernel.cu:489-501 Rel_NonCompen */
+int rtm_k_Rel_NonCompen(float *DBW2, float *DFW2, float *Drel1, float *Drel2, int NZ, int NX,
+                        rtm_stream_t s);
+/* kernel.cu:503-517 Rel_Compen */
+int rtm_k_Rel_Compen(float *DBW2, float *DFW2, float *DBWADD, float *DFWADD, float *Drel1,
+                     float *Drel2, int NZ, int NX, rtm_stream_t s);
+
+/* ======================================================================
+ * 2. Host preparation (replaces the reference's host set-up code).
+ * ====================================================================== */
+
+/* GPU_velocity_real.cpp:6-118 (velocity): vin is the interior model as the
+ * reference's velocity file stores it (column-major, nx columns of nz).
+ * Fills the padded v[NZ*NX] (edge extension, optional left/right flip) and
+ * r_1[NZ*NX] = sqrt((v*tao/h)^2/2). */
+int rtm_prep_velocity(const float *vin, int nz, int nx, int N2, float tao, float h, int flip,
+                      float *v, float *r1);
+/* kernel.cu:704-742: snapped vmin/vmax, nvel, and need[nvel] (may be NULL to
+ * query nvel; need_cap is its capacity). */
+int rtm_prep_bins(const float *v, long ncell, float dv, float *vmin, float *vmax, int *nvel,
+                  int *need, int need_cap);
+/* kernel.cu:1261-1266 (f): wav[i] = Ricker(i*tao, f0), i < n. */
+int rtm_prep_wavelet(float *wav, int n, float tao, float f0);
+/* LSMOrCon_rec_2D.cpp:526-551 (order): Taylor coefficients c[0..N/2]. */
+int rtm_prep_taylor(int N, float *c);
+
+/* ======================================================================
+ * 3. Shot level.
+ * ====================================================================== */
+
+/* One model grid shared by a batch of shots.  Host pointers; copied at
+ * rtm_ctx_create.  Coordinates are 0-based cells of the padded grid. */
+typedef struct rtm_problem {
+    int nz, nx, N2;     /* interior size and pad width (NZ = nz+2*N2, ...)      */
+    int M;              /* nfdmax: ring width and longest operator              */
+    int NT, NT2;        /* time steps; wavelet injected while step < NT2        */
+    int adaptive;       /* 1: per-velocity-bin coefficients (iLSTE=0)           */
+    int compen;         /* iCompen                                              */
+    int quirk;          /* 1: the reference's velocity indexing in the ABC      */
+    int nbins;          /* nvel (adaptive) ; ignored otherwise                  */
+    float tao2, h2, taoh, taoh2, vmin, dv, hzx2_1, spike;
+    const float *v;     /* [NZ*NX] padded velocity                               */
+    const float *r1;    /* [NZ*NX] r_1                                           */
+    const float *w;     /* [N2+1] blend weights                                  */
+    const float *coef;  /* adaptive: reference table c[Index[b] .. Index[b+1]-1];
+                           fixed: c[0..M]                                        */
+    const int *index;   /* [nbins+1] (adaptive)                                  */
+    const float *wav;   /* [NT+1] wav[i] = f(i*tao)                              */
+    /* receivers: cells (rz0 + j*rdz, rx0 + j*rdx), j < nrec (a surface line,
+       a vertical well, ...); both steps 0 is invalid */
+    int rz0, rx0, rdz, rdx, nrec;
+    int ring_precision; /* RTM_RING_F32 / RTM_RING_BF16 / RTM_RING_F16          */
+} rtm_problem;
+
+enum { RTM_RING_F32 = 0, RTM_RING_BF16 = 1, RTM_RING_F16 = 2 };
+
+/* flags for rtm_model_batch / rtm_migrate_batch */
+enum {
+    RTM_DEVICE_PTRS = 1, /* data/result pointers are device pointers            */
+    RTM_NO_GRAPH = 2     /* launch step by step instead of replaying a graph    */
+};
+
+typedef struct rtm_ctx rtm_ctx;
+
+/* max_batch: shots advanced together (device memory is sized for it). */
+int rtm_ctx_create(rtm_ctx **ctx, const rtm_problem *p, int max_batch, rtm_stream_t stream);
+int rtm_ctx_destroy(rtm_ctx *ctx);
+/* Device bytes held by the context. */
+int rtm_ctx_bytes(const rtm_ctx *ctx, size_t *bytes);
+
+/* Forward modelling with receiver recording (new relative to the reference,
+ * which reads recorded gathers from files).  src_cells[nshot] are flat
+ * padded-grid indices z*NX+x of the sources (host).  rec is trace-major
+ * [nshot][nrec][NT]. */
+int rtm_model_batch(rtm_ctx *ctx, int nshot, const int *src_cells, float *rec, int flags);
+
+/* Migration of nshot shots (kernel.cu:798-933 per shot): forward source run,
+ * boundary-ring reconstruction, receiver back-propagation with Dirichlet
+ * injection of the gathers seis [nshot][nrec][NT] (trace-major), imaging.
+ * rel1/rel2 receive the full padded cross-correlation / illumination grids
+ * [nshot][NZ][NX] (either may be NULL). */
+int rtm_migrate_batch(rtm_ctx *ctx, int nshot, const int *src_cells, const float *seis,
+                      float *rel1, float *rel2, int flags);
+
+/* Migration plus per-shot finishing (kernel.cu:935-990) and a compensated
+ * (Kahan) stack over the shots (kernel.cu:992-1059): image and illum are the
+ * interior [nz][nx] stacked results (image divided by nrec_div and, when
+ * inorm, by the stacked illumination).  ups/downs (may be NULL) receive the
+ * per-shot interior images [nshot][nz][nx]. */
+int rtm_migrate_stack(rtm_ctx *ctx, int nshot, const int *src_cells, const float *seis,
+                      float whitecoe, int nrec_div, int inorm, float *image, float *illum,
+                      float *ups, float *downs, int flags);
+
+/* Per-launch timing: with timing enabled, launches go one by one (no graph)
+ * with CUDA events around each kernel; rtm_ctx_timing returns the summed
+ * milliseconds and launch counts of [0] forward stencil, [1] backward
+ * stencil (source + receiver + imaging), [2] pad kernels. */
+int rtm_ctx_set_timing(rtm_ctx *ctx, int enable);
+int rtm_ctx_timing(const rtm_ctx *ctx, double ms[3], long n[3]);
+/* Kernels this context has launched (graph replays count their kernels). */
+int rtm_ctx_launches(rtm_ctx *ctx, long *count, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTM_GB300_H */

@@ -1,0 +1,721 @@
+// Shot-level engine: context, batched forward / backward time loops captured
+// in CUDA graphs, per-shot finishing and the compensated stack.
+//
+// Per shot (kernel.cu:791-990), for a batch of shots advancing together:
+//   forward  k = 2..NT-1 : k_step<FWD> ; k_pad (blend, ring save, record)
+//   hand-off            : k_img_init (accumulator initialisation)
+//   backward k = NT-3..0 : k_step<BWD> (source reconstruction + receiver
+//                          propagation + imaging) ; k_pad (receiver blend,
+//                          ring restore of the source field)
+// Levels rotate through three buffers by index (level k lives in buffer
+// k % 3), so the reference's copy kernels (Deliver, Deliver_EFF) disappear.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "rtm_engine_kernels.cuh"
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+int make_map(CUtensorMap *m, float *base, int NX, int NZ, int B, int P, int bw, int bh)
+{
+    auto enc = get_encode();
+    if (!enc) {
+        rtm_set_last_error("cuTensorMapEncodeTiled unavailable");
+        return RTM_ERR_CUDA;
+    }
+    cuuint64_t dims[3] = {(cuuint64_t)NX, (cuuint64_t)NZ, (cuuint64_t)B};
+    cuuint64_t strides[2] = {(cuuint64_t)P * 4, (cuuint64_t)P * 4 * NZ};
+    cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        rtm_set_last_error("cuTensorMapEncodeTiled failed");
+        return RTM_ERR_CUDA;
+    }
+    return RTM_OK;
+}
+
+inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace
+
+struct rtm_ctx {
+    rtm_problem p{};
+    int NZ = 0, NX = 0, P = 0, nz = 0, nx = 0, N2 = 0, M = 0, MM = 0, B = 0, NT = 0, nrec = 0;
+    long long ss = 0;       // floats per shot grid
+    long ringsz = 0;        // cells per ring slot
+    cudaStream_t st = nullptr;
+    bool own_stream = false;  // created by the context (graphs cannot capture the legacy stream)
+    std::vector<float> wav; // host wavelet table
+    float vmax = 0.f;
+    int nbins = 1;
+    // device
+    float *v = nullptr, *r1 = nullptr, *w = nullptr, *ctab = nullptr;
+    float *S[3] = {nullptr, nullptr, nullptr}, *R[3] = {nullptr, nullptr, nullptr};
+    float *pre = nullptr, *rel1 = nullptr, *rel2 = nullptr, *sacc = nullptr, *racc = nullptr;
+    float *ring = nullptr, *data = nullptr, *rec = nullptr, *stage = nullptr;
+    int *src = nullptr;
+    unsigned *imax = nullptr;
+    float *ups = nullptr, *downs = nullptr;                       // per-batch finished images
+    float *ks1 = nullptr, *kc1 = nullptr, *ks2 = nullptr, *kc2 = nullptr;  // Kahan state
+    float *img = nullptr, *ill = nullptr;
+    CUtensorMap mapS[3], mapR[3];
+    size_t bytes = 0;
+    // graphs keyed by (phase, batch)
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    double ms_stencil = 0, ms_pad = 0, ms_bwd = 0;
+    long n_stencil = 0, n_pad = 0, n_bwd = 0;
+    // kernels launched (graph replays count their kernels)
+    long launches = 0;
+    std::map<std::pair<int, int>, long> graph_kernels;
+};
+
+namespace {
+
+template <class T>
+int dalloc(rtm_ctx *c, T **p, size_t n)
+{
+    if (n == 0) n = 1;
+    if (cudaMalloc(p, n * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        rtm_set_last_error("cudaMalloc failed");
+        return RTM_ERR_NOMEM;
+    }
+    c->bytes += n * sizeof(T);
+    if (cudaMemset(*p, 0, n * sizeof(T)) != cudaSuccess) return RTM_ERR_CUDA;
+    return RTM_OK;
+}
+
+void free_all(rtm_ctx *c)
+{
+    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    float *fl[] = {c->v, c->r1, c->w, c->ctab, c->S[0], c->S[1], c->S[2], c->R[0], c->R[1], c->R[2],
+                   c->pre, c->rel1, c->rel2, c->sacc, c->racc, c->ring, c->data, c->rec, c->stage,
+                   c->ups, c->downs, c->ks1, c->kc1, c->ks2, c->kc2, c->img, c->ill};
+    for (float *p : fl)
+        if (p) cudaFree(p);
+    if (c->src) cudaFree(c->src);
+    if (c->imax) cudaFree(c->imax);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->own_stream && c->st) {
+        cudaStreamDestroy(c->st);
+        c->st = nullptr;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+
+using StepFn = void (*)(const CUtensorMap, const CUtensorMap, const eng::StepArgs);
+
+template <int MMAX, bool AD, int MODE>
+int launch_step_t(rtm_ctx *c, const CUtensorMap &mA, const CUtensorMap &mS,
+                  const eng::StepArgs &a, int nb)
+{
+    using S = eng::Shape<MMAX>;
+    const unsigned smem = S::BYTES * (MODE == eng::MODE_BWD ? 2u : 1u) + 16u;
+    dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
+    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(mA, mS, a);
+    return RTM_OK;
+}
+
+template <int MMAX, bool AD, int MODE>
+void set_attr_t()
+{
+    using S = eng::Shape<MMAX>;
+    const int smem = (int)(S::BYTES * (MODE == eng::MODE_BWD ? 2u : 1u) + 16u);
+    cudaFuncSetAttribute(eng::k_step<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+template <int MMAX>
+void set_attr_m()
+{
+    set_attr_t<MMAX, true, eng::MODE_FWD>();
+    set_attr_t<MMAX, false, eng::MODE_FWD>();
+    set_attr_t<MMAX, true, eng::MODE_BWD>();
+    set_attr_t<MMAX, false, eng::MODE_BWD>();
+}
+
+void init_step_attrs()
+{
+    static bool done = false;
+    if (done) return;
+    set_attr_m<4>();
+    set_attr_m<8>();
+    set_attr_m<12>();
+    done = true;
+}
+
+template <int MMAX>
+int launch_step_m(rtm_ctx *c, int mode, const CUtensorMap &mA, const CUtensorMap &mS,
+                  const eng::StepArgs &a, int nb)
+{
+    const bool ad = c->p.adaptive != 0;
+    if (mode == eng::MODE_FWD)
+        return ad ? launch_step_t<MMAX, true, eng::MODE_FWD>(c, mA, mS, a, nb)
+                  : launch_step_t<MMAX, false, eng::MODE_FWD>(c, mA, mS, a, nb);
+    return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, mA, mS, a, nb)
+              : launch_step_t<MMAX, false, eng::MODE_BWD>(c, mA, mS, a, nb);
+}
+
+int launch_step(rtm_ctx *c, int mode, const CUtensorMap &mA, const CUtensorMap &mS,
+                const eng::StepArgs &a, int nb)
+{
+    switch (c->MM) {
+    case 4: return launch_step_m<4>(c, mode, mA, mS, a, nb);
+    case 8: return launch_step_m<8>(c, mode, mA, mS, a, nb);
+    case 12: return launch_step_m<12>(c, mode, mA, mS, a, nb);
+    default: rtm_set_last_error("unsupported operator length"); return RTM_ERR_UNSUPPORTED;
+    }
+}
+
+eng::StepArgs base_step(rtm_ctx *c)
+{
+    eng::StepArgs a{};
+    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2; a.nbins = c->nbins;
+    a.ss = c->ss;
+    a.vmin = c->p.vmin; a.dv = c->p.dv; a.tao2 = c->p.tao2; a.h2 = c->p.h2;
+    a.k0 = (float)(1.0 + (double)c->p.hzx2_1);
+    a.hzx2_1 = c->p.hzx2_1;
+    a.v = c->v; a.ctab = c->ctab; a.src = c->src; a.compen = c->p.compen;
+    a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = 0;
+    a.rel1 = c->rel1; a.rel2 = c->rel2; a.sacc = c->sacc; a.racc = c->racc;
+    return a;
+}
+
+eng::PadArgs base_pad(rtm_ctx *c)
+{
+    eng::PadArgs a{};
+    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2; a.M = c->M; a.nz = c->nz; a.nx = c->nx;
+    a.quirk = c->p.quirk; a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
+    a.taoh = c->p.taoh; a.taoh2 = c->p.taoh2; a.v = c->v; a.r1 = c->r1; a.w = c->w;
+    a.pre = c->pre;
+    a.ring_ss = (long long)c->NT * c->ringsz;
+    a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = c->nrec;
+    return a;
+}
+
+void tic(rtm_ctx *c)
+{
+    if (c->timing) cudaEventRecord(c->ev[0], c->st);
+}
+// kind: 0 forward stencil, 1 backward stencil, 2 pad kernel
+void toc(rtm_ctx *c, int kind)
+{
+    c->launches++;
+    if (!c->timing) return;
+    cudaEventRecord(c->ev[1], c->st);
+    cudaEventSynchronize(c->ev[1]);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    if (kind == 0) { c->ms_stencil += ms; c->n_stencil++; }
+    else if (kind == 1) { c->ms_bwd += ms; c->n_bwd++; }
+    else { c->ms_pad += ms; c->n_pad++; }
+}
+
+// Forward run of nb shots (sources already in c->src).  rec_on: record the
+// receivers into c->rec (time-major [shot][NT][nrec]).
+int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
+{
+    const long long ss = c->ss;
+    const int NT = c->NT;
+    eng::k_shot_init<<<dim3(cdiv(ss, 256), nb), 256, 0, c->st>>>(c->S[0], c->S[1], c->S[2], c->pre,
+                                                                 c->src, c->p.spike, ss, c->NX, c->P);
+    c->launches++;
+    if (c->M > 0)
+        eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
+            c->S[1], c->ring + c->ringsz, ss, (long long)NT * c->ringsz, c->NZ, c->NX, c->P, c->N2, c->M);
+    c->launches += (c->M > 0);
+    const long long rss = (long long)NT * c->nrec;
+    if (rec_on && c->nrec > 0) {
+        eng::k_record<<<dim3(cdiv(c->nrec, 128), nb), 128, 0, c->st>>>(
+            c->S[0], c->rec, ss, rss, c->P, c->p.rz0, c->p.rx0, c->p.rdz, c->p.rdx, c->nrec);
+        c->launches++;
+    }
+    RTM_LAUNCH_CHECK();
+    eng::StepArgs sa = base_step(c);
+    eng::PadArgs pa = base_pad(c);
+    const long npad = abc_count(c->NZ, c->NX, c->N2) + (rec_on ? c->nrec : 0);
+    for (int k = 2; k < NT; ++k) {
+        float *a0 = c->S[(k - 2) % 3], *a1 = c->S[(k - 1) % 3], *a2 = c->S[k % 3];
+        sa.a0 = a0; sa.a2 = a2; sa.pre = c->pre;
+        sa.wavelet = (k < c->p.NT2) ? c->wav[k - 1] : 0.0f;
+        tic(c);
+        if (int rc = launch_step(c, eng::MODE_FWD, c->mapS[(k - 1) % 3], c->mapS[(k - 1) % 3], sa, nb))
+            return rc;
+        toc(c, 0);
+        pa.a0 = a0; pa.a1 = a1; pa.a2 = a2;
+        pa.ring_mode = c->M > 0 ? 1 : 0;
+        pa.ring = c->ring + (long long)k * c->ringsz;
+        pa.rec = rec_on ? c->rec + (long long)(k - 1) * c->nrec : nullptr;
+        pa.rec_ss = rss;
+        tic(c);
+        eng::k_pad<<<dim3(cdiv(npad, 256), nb), 256, 0, c->st>>>(pa);
+        toc(c, 2);
+    }
+    if (rec_on && c->nrec > 0)
+        eng::k_record<<<dim3(cdiv(c->nrec, 128), nb), 128, 0, c->st>>>(
+            c->S[(NT - 1) % 3], c->rec + (long long)(NT - 1) * c->nrec, ss, rss, c->P, c->p.rz0,
+            c->p.rx0, c->p.rdz, c->p.rdx, c->nrec);
+    c->launches += (rec_on && c->nrec > 0);
+    RTM_LAUNCH_CHECK();
+    return RTM_OK;
+}
+
+// Backward pass of nb shots (after enqueue_forward; observed data in c->data
+// time-major [shot][NT][nrec]).
+int enqueue_backward(rtm_ctx *c, int nb)
+{
+    const long long ss = c->ss;
+    const int NT = c->NT;
+    float *F1 = c->S[(NT - 1) % 3], *F0 = c->S[(NT - 2) % 3];
+    eng::k_img_init<<<dim3(cdiv(ss, 256), nb), 256, 0, c->st>>>(
+        F1, F0, c->R[0], c->R[1], c->R[2], c->rel1, c->rel2, c->sacc, c->racc, c->src, c->p.spike,
+        c->p.compen, ss, c->NX, c->P);
+    c->launches++;
+    RTM_LAUNCH_CHECK();
+    eng::StepArgs sa = base_step(c);
+    sa.nrec = c->nrec;
+    sa.dstride = (long long)NT * c->nrec;
+    eng::PadArgs pa = base_pad(c);
+    const long npad = abc_count(c->NZ, c->NX, c->N2);
+    for (int k = NT - 3; k >= 0; --k) {
+        const int i2 = k % 3, i1 = (k + 1) % 3, i0 = (k + 2) % 3;
+        sa.a0 = c->R[i0]; sa.a2 = c->R[i2]; sa.pre = c->pre;
+        sa.s0 = c->S[i0]; sa.s2 = c->S[i2];
+        sa.wavelet = (k < c->p.NT2) ? c->wav[k + 1] : 0.0f;
+        sa.dinj = c->data + (long long)(k + 1) * c->nrec;
+        tic(c);
+        if (int rc = launch_step(c, eng::MODE_BWD, c->mapR[i1], c->mapS[i1], sa, nb)) return rc;
+        toc(c, 1);
+        pa.a0 = c->R[i0]; pa.a1 = c->R[i1]; pa.a2 = c->R[i2];
+        pa.ring_mode = c->M > 0 ? 2 : 0;
+        pa.ring = c->ring + (long long)k * c->ringsz;
+        pa.s2 = c->S[i2];
+        pa.rec = nullptr;
+        tic(c);
+        eng::k_pad<<<dim3(cdiv(npad, 256), nb), 256, 0, c->st>>>(pa);
+        toc(c, 2);
+    }
+    RTM_LAUNCH_CHECK();
+    return RTM_OK;
+}
+
+// Runs phase (0 forward+record, 1 forward+backward) for nb shots, through a
+// cached CUDA graph unless timing is on or RTM_NO_GRAPH is given.
+int run_phase(rtm_ctx *c, int phase, int nb, int flags)
+{
+    const bool use_graph = !(flags & RTM_NO_GRAPH) && !c->timing;
+    auto body = [&]() -> int {
+        if (phase == 0) return enqueue_forward(c, nb, true);
+        if (int rc = enqueue_forward(c, nb, false)) return rc;
+        return enqueue_backward(c, nb);
+    };
+    if (!use_graph) return body();
+    auto key = std::make_pair(phase, nb);
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+        cudaGraph_t g;
+        RTM_CUDA_TRY(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        const long before = c->launches;
+        int rc = body();
+        c->graph_kernels[key] = c->launches - before;
+        c->launches = before;
+        cudaError_t e = cudaStreamEndCapture(c->st, &g);
+        if (rc) {
+            if (e == cudaSuccess) cudaGraphDestroy(g);
+            return rc;
+        }
+        RTM_CUDA_TRY(e);
+        cudaGraphExec_t ge;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        RTM_CUDA_TRY(e);
+        it = c->graphs.emplace(key, ge).first;
+    }
+    RTM_CUDA_TRY(cudaGraphLaunch(it->second, c->st));
+    c->launches += c->graph_kernels[key];
+    return RTM_OK;
+}
+
+int upload_src(rtm_ctx *c, int nb, const int *src_cells)
+{
+    for (int i = 0; i < nb; ++i) {
+        const int s = src_cells[i];
+        if (s < 0 || s >= c->NZ * c->NX) {
+            rtm_set_last_error("source cell outside the grid");
+            return RTM_ERR_ARG;
+        }
+    }
+    RTM_CUDA_TRY(cudaMemcpyAsync(c->src, src_cells, sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
+    return RTM_OK;
+}
+
+// [nb][nrec][NT] (trace-major) <-> [nb][NT][nrec] (time-major)
+__global__ void k_transpose(const float *in, float *out, int rows, int cols, long long per)
+{
+    __shared__ float t[32][33];
+    const int shot = blockIdx.z;
+    const float *I = in + shot * per;
+    float *O = out + shot * per;
+    int c = blockIdx.x * 32 + threadIdx.x, r = blockIdx.y * 32 + threadIdx.y;
+    for (int j = 0; j < 32; j += 8)
+        if (r + j < rows && c < cols) t[threadIdx.y + j][threadIdx.x] = I[(long)(r + j) * cols + c];
+    __syncthreads();
+    c = blockIdx.y * 32 + threadIdx.x;
+    r = blockIdx.x * 32 + threadIdx.y;
+    for (int j = 0; j < 32; j += 8)
+        if (r + j < cols && c < rows) O[(long)(r + j) * rows + c] = t[threadIdx.x][threadIdx.y + j];
+}
+
+void transpose(rtm_ctx *c, const float *in, float *out, int rows, int cols, int nb)
+{
+    dim3 g(cdiv(cols, 32), cdiv(rows, 32), nb);
+    k_transpose<<<g, dim3(32, 8), 0, c->st>>>(in, out, rows, cols, (long long)rows * cols);
+    c->launches++;
+}
+
+// full padded grid [nb][NZ][P] -> [nb][NZ][NX]
+int copy_grid_out(rtm_ctx *c, const float *dsrc, float *dst, int nb, bool dev)
+{
+    RTM_CUDA_TRY(cudaMemcpy2DAsync(dst, sizeof(float) * c->NX, dsrc, sizeof(float) * c->P,
+                                   sizeof(float) * c->NX, (size_t)c->NZ * nb,
+                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+    return RTM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rtm_device_error(unsigned int *code)
+{
+    unsigned v = 0, z = 0;
+    RTM_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_rtm_dev_error, sizeof(v)));
+    RTM_CUDA_TRY(cudaMemcpyToSymbol(g_rtm_dev_error, &z, sizeof(z)));
+    if (code) *code = v;
+    return RTM_OK;
+}
+
+int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_stream_t stream)
+{
+    if (!out || !p || max_batch < 1) return RTM_ERR_ARG;
+    *out = nullptr;
+    if (p->nz < 1 || p->nx < 1 || p->N2 < 2 || p->M < 0 || p->M > p->N2 || p->NT < 4 || !p->v ||
+        !p->r1 || !p->w || !p->coef || !p->wav || (p->adaptive && (!p->index || p->nbins < 1)) ||
+        p->ring_precision != RTM_RING_F32) {
+        rtm_set_last_error("rtm_ctx_create: invalid problem");
+        return RTM_ERR_ARG;
+    }
+    if (p->nrec > 0 && p->rdz == 0 && p->rdx == 0) {
+        rtm_set_last_error("rtm_ctx_create: receiver step is zero");
+        return RTM_ERR_ARG;
+    }
+    rtm_ctx *c = new rtm_ctx();
+    c->p = *p;
+    c->nz = p->nz; c->nx = p->nx; c->N2 = p->N2; c->M = p->M; c->NT = p->NT;
+    c->NZ = p->nz + 2 * p->N2; c->NX = p->nx + 2 * p->N2;
+    c->P = (c->NX + eng::TX - 1) / eng::TX * eng::TX;
+    c->B = max_batch;
+    c->nrec = p->nrec;
+    c->ss = (long long)c->NZ * c->P;
+    c->ringsz = 2L * c->M * (c->nx + c->nz);
+    for (int j = 0; j < p->nrec; ++j) {
+        const int z = p->rz0 + j * p->rdz, x = p->rx0 + j * p->rdx;
+        if (z < 0 || z >= c->NZ || x < 0 || x >= c->NX) {
+            rtm_set_last_error("receiver outside the grid");
+            delete c;
+            return RTM_ERR_ARG;
+        }
+    }
+    // operator length of the kernels: every bin's length padded to MM
+    int mlen = p->M;
+    std::vector<float> tab;
+    if (p->adaptive) {
+        mlen = 0;
+        for (int b = 0; b < p->nbins; ++b) mlen = std::max(mlen, p->index[b + 1] - p->index[b] - 1);
+    }
+    c->MM = mlen <= 4 ? 4 : (mlen <= 8 ? 8 : (mlen <= 12 ? 12 : 0));
+    if (c->MM == 0 || mlen > p->N2) {
+        rtm_set_last_error("operator length above 12 or above the pad width");
+        delete c;
+        return RTM_ERR_UNSUPPORTED;
+    }
+    if (c->NZ < 2 * c->MM + 2 || c->NX < 2 * c->MM + 2) {
+        rtm_set_last_error("grid smaller than the operator");
+        delete c;
+        return RTM_ERR_ARG;
+    }
+    init_step_attrs();
+    if (stream) {
+        c->st = stream;
+    } else if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+        rtm_set_last_error("cudaStreamCreate failed");
+        delete c;
+        return RTM_ERR_CUDA;
+    } else {
+        c->own_stream = true;
+    }
+    if (p->adaptive) {
+        c->nbins = p->nbins;
+        tab.assign((size_t)(c->MM + 1) * c->nbins, 0.0f);
+        for (int b = 0; b < p->nbins; ++b)
+            for (int l = 0; l < p->index[b + 1] - p->index[b]; ++l)
+                tab[(size_t)l * c->nbins + b] = p->coef[p->index[b] + l];
+    } else {
+        c->nbins = 1;
+        tab.assign(c->MM + 1, 0.0f);
+        for (int l = 0; l <= p->M; ++l) tab[l] = p->coef[l];
+    }
+    c->wav.assign(p->wav, p->wav + p->NT + 1);
+    int rc = RTM_OK;
+    const size_t grid = (size_t)c->ss;
+    const size_t bgrid = grid * c->B;
+#define TRY(x)                     \
+    do {                           \
+        if ((rc = (x)) != RTM_OK) { \
+            free_all(c);           \
+            delete c;              \
+            return rc;             \
+        }                          \
+    } while (0)
+    TRY(dalloc(c, &c->v, grid));
+    TRY(dalloc(c, &c->r1, grid));
+    TRY(dalloc(c, &c->w, (size_t)c->N2 + 1));
+    TRY(dalloc(c, &c->ctab, tab.size()));
+    for (int i = 0; i < 3; ++i) {
+        TRY(dalloc(c, &c->S[i], bgrid));
+        TRY(dalloc(c, &c->R[i], bgrid));
+    }
+    TRY(dalloc(c, &c->pre, bgrid));
+    TRY(dalloc(c, &c->rel1, bgrid));
+    TRY(dalloc(c, &c->rel2, bgrid));
+    TRY(dalloc(c, &c->sacc, bgrid));
+    TRY(dalloc(c, &c->racc, bgrid));
+    TRY(dalloc(c, &c->ring, (size_t)c->B * c->NT * std::max<long>(c->ringsz, 1)));
+    TRY(dalloc(c, &c->data, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
+    TRY(dalloc(c, &c->rec, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
+    TRY(dalloc(c, &c->stage, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
+    TRY(dalloc(c, &c->src, (size_t)c->B));
+    TRY(dalloc(c, &c->imax, (size_t)c->B));
+    TRY(dalloc(c, &c->ups, (size_t)c->B * c->nz * c->nx));
+    TRY(dalloc(c, &c->downs, (size_t)c->B * c->nz * c->nx));
+    for (float **q : {&c->ks1, &c->kc1, &c->ks2, &c->kc2, &c->img, &c->ill})
+        TRY(dalloc(c, q, (size_t)c->nz * c->nx));
+    // model: padded rows, pad columns of each row hold the row's last value so
+    // that bins computed there stay in range
+    {
+        std::vector<float> hv((size_t)grid), hr((size_t)grid);
+        for (int z = 0; z < c->NZ; ++z)
+            for (int x = 0; x < c->P; ++x) {
+                const int xs = std::min(x, c->NX - 1);
+                hv[(size_t)z * c->P + x] = p->v[(size_t)z * c->NX + xs];
+                hr[(size_t)z * c->P + x] = p->r1[(size_t)z * c->NX + xs];
+            }
+        float vmx = p->v[0];
+        for (long i = 0; i < (long)c->NZ * c->NX; ++i) vmx = std::max(vmx, p->v[i]);
+        c->vmax = vmx;
+        if (cudaMemcpy(c->v, hv.data(), grid * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(c->r1, hr.data(), grid * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(c->w, p->w, (c->N2 + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(c->ctab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+            rtm_set_last_error("upload failed");
+            free_all(c);
+            delete c;
+            return RTM_ERR_CUDA;
+        }
+    }
+    int bw = 0, bh = 0;
+    switch (c->MM) {
+    case 4: bw = eng::Shape<4>::BW; bh = eng::Shape<4>::BH; break;
+    case 8: bw = eng::Shape<8>::BW; bh = eng::Shape<8>::BH; break;
+    default: bw = eng::Shape<12>::BW; bh = eng::Shape<12>::BH; break;
+    }
+    for (int i = 0; i < 3; ++i) {
+        TRY(make_map(&c->mapS[i], c->S[i], c->NX, c->NZ, c->B, c->P, bw, bh));
+        TRY(make_map(&c->mapR[i], c->R[i], c->NX, c->NZ, c->B, c->P, bw, bh));
+    }
+#undef TRY
+    cudaEventCreate(&c->ev[0]);
+    cudaEventCreate(&c->ev[1]);
+    *out = c;
+    return RTM_OK;
+}
+
+int rtm_ctx_destroy(rtm_ctx *c)
+{
+    if (!c) return RTM_OK;
+    cudaStreamSynchronize(c->st);
+    free_all(c);
+    delete c;
+    return RTM_OK;
+}
+
+int rtm_ctx_bytes(const rtm_ctx *c, size_t *bytes)
+{
+    if (!c || !bytes) return RTM_ERR_ARG;
+    *bytes = c->bytes;
+    return RTM_OK;
+}
+
+int rtm_ctx_set_timing(rtm_ctx *c, int enable)
+{
+    if (!c) return RTM_ERR_ARG;
+    c->timing = enable != 0;
+    c->ms_stencil = c->ms_pad = c->ms_bwd = 0;
+    c->n_stencil = c->n_pad = c->n_bwd = 0;
+    return RTM_OK;
+}
+
+int rtm_ctx_timing(const rtm_ctx *c, double ms[3], long n[3])
+{
+    if (!c || !ms || !n) return RTM_ERR_ARG;
+    ms[0] = c->ms_stencil; ms[1] = c->ms_bwd; ms[2] = c->ms_pad;
+    n[0] = c->n_stencil; n[1] = c->n_bwd; n[2] = c->n_pad;
+    return RTM_OK;
+}
+
+int rtm_ctx_launches(rtm_ctx *c, long *count, int reset)
+{
+    if (!c || !count) return RTM_ERR_ARG;
+    *count = c->launches;
+    if (reset) c->launches = 0;
+    return RTM_OK;
+}
+
+int rtm_model_batch(rtm_ctx *c, int nshot, const int *src_cells, float *rec, int flags)
+{
+    if (!c || nshot < 0 || (nshot > 0 && (!src_cells || !rec))) return RTM_ERR_ARG;
+    const bool dev = flags & RTM_DEVICE_PTRS;
+    const long long per = (long long)c->NT * c->nrec;
+    for (int s0 = 0; s0 < nshot; s0 += c->B) {
+        const int nb = std::min(c->B, nshot - s0);
+        if (int rc = upload_src(c, nb, src_cells + s0)) return rc;
+        if (int rc = run_phase(c, 0, nb, flags)) return rc;
+        if (c->nrec > 0) {
+            transpose(c, c->rec, c->stage, c->NT, c->nrec, nb);
+            RTM_CUDA_TRY(cudaMemcpyAsync(rec + (long long)s0 * per, c->stage, sizeof(float) * per * nb,
+                                         dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+        }
+    }
+    RTM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    unsigned e = 0;
+    rtm_device_error(&e);
+    if (e) {
+        rtm_set_last_error("device-side wait timed out");
+        return RTM_ERR_DEVICE;
+    }
+    return RTM_OK;
+}
+
+static int migrate_group(rtm_ctx *c, int s0, int nb, const int *src_cells, const float *seis, int flags)
+{
+    const bool dev = flags & RTM_DEVICE_PTRS;
+    const long long per = (long long)c->NT * c->nrec;
+    if (int rc = upload_src(c, nb, src_cells + s0)) return rc;
+    if (c->nrec > 0) {
+        RTM_CUDA_TRY(cudaMemcpyAsync(c->stage, seis + (long long)s0 * per, sizeof(float) * per * nb,
+                                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
+        transpose(c, c->stage, c->data, c->nrec, c->NT, nb);
+    }
+    return run_phase(c, 1, nb, flags);
+}
+
+int rtm_migrate_batch(rtm_ctx *c, int nshot, const int *src_cells, const float *seis, float *rel1,
+                      float *rel2, int flags)
+{
+    if (!c || nshot < 0 || (nshot > 0 && (!src_cells || (!seis && c->nrec > 0)))) return RTM_ERR_ARG;
+    const bool dev = flags & RTM_DEVICE_PTRS;
+    const long long gsz = (long long)c->NZ * c->NX;
+    for (int s0 = 0; s0 < nshot; s0 += c->B) {
+        const int nb = std::min(c->B, nshot - s0);
+        if (int rc = migrate_group(c, s0, nb, src_cells, seis, flags)) return rc;
+        if (rel1)
+            if (int rc = copy_grid_out(c, c->rel1, rel1 + s0 * gsz, nb, dev)) return rc;
+        if (rel2)
+            if (int rc = copy_grid_out(c, c->rel2, rel2 + s0 * gsz, nb, dev)) return rc;
+    }
+    RTM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    unsigned e = 0;
+    rtm_device_error(&e);
+    if (e) {
+        rtm_set_last_error("device-side wait timed out");
+        return RTM_ERR_DEVICE;
+    }
+    return RTM_OK;
+}
+
+int rtm_migrate_stack(rtm_ctx *c, int nshot, const int *src_cells, const float *seis,
+                      float whitecoe, int nrec_div, int inorm, float *image, float *illum,
+                      float *ups, float *downs, int flags)
+{
+    if (!c || nshot < 1 || !src_cells || (!seis && c->nrec > 0) || nrec_div < 1) return RTM_ERR_ARG;
+    const bool dev = flags & RTM_DEVICE_PTRS;
+    const long ncell = (long)c->nz * c->nx;
+    for (float *q : {c->ks1, c->kc1, c->ks2, c->kc2})
+        RTM_CUDA_TRY(cudaMemsetAsync(q, 0, sizeof(float) * ncell, c->st));
+    for (int s0 = 0; s0 < nshot; s0 += c->B) {
+        const int nb = std::min(c->B, nshot - s0);
+        if (int rc = migrate_group(c, s0, nb, src_cells, seis, flags)) return rc;
+        RTM_CUDA_TRY(cudaMemsetAsync(c->imax, 0, sizeof(unsigned) * nb, c->st));
+        eng::k_illum_max<<<dim3(64, nb), 256, 0, c->st>>>(c->rel2, c->imax, c->ss, c->NZ, c->NX, c->P,
+                                                          c->N2);
+        eng::k_finish<<<dim3(cdiv(ncell, 256), nb), 256, 0, c->st>>>(
+            c->rel1, c->rel2, c->v, c->imax, c->ups, c->downs, c->ss, c->NZ, c->NX, c->P, c->N2,
+            c->vmax, whitecoe);
+        eng::k_stack_kahan<<<cdiv(ncell, 256), 256, 0, c->st>>>(c->ups, c->downs, nb, ncell, c->ks1,
+                                                               c->kc1, c->ks2, c->kc2);
+        c->launches += 3;
+        RTM_LAUNCH_CHECK();
+        const auto kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (ups)
+            RTM_CUDA_TRY(cudaMemcpyAsync(ups + (long long)s0 * ncell, c->ups, sizeof(float) * ncell * nb,
+                                         kind, c->st));
+        if (downs)
+            RTM_CUDA_TRY(cudaMemcpyAsync(downs + (long long)s0 * ncell, c->downs,
+                                         sizeof(float) * ncell * nb, kind, c->st));
+    }
+    eng::k_stack_final<<<cdiv(ncell, 256), 256, 0, c->st>>>(c->ks1, c->ks2, c->img, c->ill, ncell,
+                                                            nrec_div, inorm);
+    c->launches++;
+    RTM_LAUNCH_CHECK();
+    const auto kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (image) RTM_CUDA_TRY(cudaMemcpyAsync(image, c->img, sizeof(float) * ncell, kind, c->st));
+    if (illum) RTM_CUDA_TRY(cudaMemcpyAsync(illum, c->ill, sizeof(float) * ncell, kind, c->st));
+    RTM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    unsigned e = 0;
+    rtm_device_error(&e);
+    if (e) {
+        rtm_set_last_error("device-side wait timed out");
+        return RTM_ERR_DEVICE;
+    }
+    return RTM_OK;
+}
+
+}  // extern "C"

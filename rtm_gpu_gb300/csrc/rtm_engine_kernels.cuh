@@ -1,0 +1,579 @@
+// Device kernels of the shot-level engine.
+//
+// Data layout (per context, in HBM):
+//   * every wavefield / image array is [shot][NZ][P] fp32 with a row pitch
+//     P = NX rounded up to the tile width (128 floats), so tiles never leave
+//     a row and every row starts on a 512-byte boundary; shots of a batch are
+//     contiguous, so a batch is one 3-D tensor {NX, NZ, B} (row stride P)
+//     that one TMA descriptor covers;
+//   * the model (v, r_1) is one [NZ][P] grid shared by the batch;
+//   * coefficients: one coefficient-major table ctab[(l)*nbins + bin],
+//     zero-padded to the compile-time operator length MMAX, so every cell runs
+//     the same unrolled loop (adding 0*x leaves a sum unchanged);
+//   * boundary rings: [shot][NT][ring] with ring = 2M(nx+nz) cells
+//     (top band M*nx, bottom band M*nx, left band M*nz, right band M*nz).
+//
+// One time step of a batch is two launches:
+//   k_step  : the 2M-order update of every cell, u1 staged in shared memory by
+//             one TMA box per tile (halo included), z-neighbours streamed
+//             through a register queue, x-neighbours read as 128-bit shared
+//             loads.  Pad cells write their pre-blend value to `pre`, interior
+//             cells write the result.  The backward variant also advances the
+//             reconstructed source field on the interior and updates the
+//             imaging accumulators of every interior cell in the same pass.
+//   k_pad   : one-way update + blend of every pad cell (reading pre-blend
+//             values from `pre`), ring save (forward) or ring restore of the
+//             source field (backward), receiver recording (forward).
+#pragma once
+
+#include "rtm_common.cuh"
+
+// Device-side error word of the engine (zero = fine); read and cleared by
+// rtm_device_error().  This header is included by one translation unit only.
+__device__ unsigned int g_rtm_dev_error = 0;
+
+namespace eng {
+
+constexpr int TX = 128;             // tile width: 32 lanes x 4 cells
+constexpr int WARPS = 4;            // warps per CTA
+constexpr int RW = 8;               // rows per warp (z streaming length)
+constexpr int TZ = WARPS * RW;      // tile height
+constexpr int NTHREADS = WARPS * 32;
+
+template <int MMAX>
+struct Shape {
+    static constexpr int XH = (MMAX + 3) / 4 * 4;  // x halo (16-byte aligned)
+    static constexpr int ZH = MMAX;                // z halo
+    static constexpr int BW = TX + 2 * XH;         // box width (floats)
+    static constexpr int BH = TZ + 2 * ZH;         // box height (rows)
+    static constexpr int ELEMS = BW * BH;
+    static constexpr unsigned BYTES = ELEMS * 4u;
+};
+
+enum { MODE_FWD = 0, MODE_BWD = 1 };
+
+struct StepArgs {
+    int NZ, NX, P, N2, nbins;
+    long long ss;              // floats between consecutive shots
+    float vmin, dv, tao2, h2, k0, hzx2_1;
+    const float *v;            // [NZ][P]
+    const float *ctab;         // [(MMAX+1)][nbins]
+    const float *a0;           // field A (u forward / R backward), level k-2
+    float *a2;                 // field A output (interior cells)
+    float *pre;                // pre-blend values of pad cells
+    const float *s0;           // backward source field, level k+2
+    float *s2;                 // backward source field output (interior)
+    float *rel1, *rel2, *sacc, *racc;
+    int compen;
+    const int *src;            // [B] flat z*NX + x
+    float wavelet;
+    int src_on_a;              // forward: source goes into field A
+    // receiver line (Dirichlet injection into field A, backward)
+    int rz0, rx0, rdz, rdx, nrec;
+    const float *dinj;         // data row for this step, shot 0; shot s at + s*dstride
+    long long dstride;
+};
+
+__device__ __forceinline__ int mirror_i(int i, int n)
+{
+    return i < 0 ? -i : (i >= n ? 2 * n - 2 - i : i);
+}
+
+// Mirror the out-of-grid halo of a staged box (the reference reflects
+// neighbour indices at the array edges, kernel.cu:65-68).  Only the tile's
+// own rows need x-halo values and only its own columns need z-halo values.
+template <int MMAX>
+__device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int NZ)
+{
+    using S = Shape<MMAX>;
+    const int gx0 = x0 - S::XH, gz0 = z0 - S::ZH;
+    // x reflection on the tile's in-grid rows, z reflection on its in-grid
+    // columns: the written and the read cells of the two passes never overlap.
+    if (x0 == 0 || x0 + TX + S::XH > NX) {
+        for (int idx = threadIdx.x; idx < TZ * S::BW; idx += NTHREADS) {
+            const int r = S::ZH + idx / S::BW, c = idx % S::BW;
+            const int gx = gx0 + c, gz = gz0 + r;
+            if ((gx >= 0 && gx < NX) || gz >= NZ) continue;
+            const int sc = mirror_i(gx, NX) - gx0;
+            t[r * S::BW + c] = (sc >= 0 && sc < S::BW) ? t[r * S::BW + sc] : 0.0f;
+        }
+    }
+    if (z0 == 0 || z0 + TZ + S::ZH > NZ) {
+        for (int idx = threadIdx.x; idx < S::BH * TX; idx += NTHREADS) {
+            const int r = idx / TX, c = S::XH + idx % TX;
+            const int gz = gz0 + r, gx = gx0 + c;
+            if ((gz >= 0 && gz < NZ) || gx >= NX) continue;
+            const int sr = mirror_i(gz, NZ) - gz0;
+            t[r * S::BW + c] = (sr >= 0 && sr < S::BH) ? t[sr * S::BW + c] : 0.0f;
+        }
+    }
+}
+
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float f4get(const float4 &v, int k)
+{
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ void f4set(float4 &v, int k, float a)
+{
+    if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
+}
+
+// Stream one field over the warp's RW rows.  For each row with z < NZ, the
+// lane's 4 cells get u2 = 2u1 - u0 + v^2 tao^2/h^2 * L(u1) and `emit` is
+// called with the results.  `q` is the register queue of rows z-M .. z+M.
+template <int MMAX, bool ADAPT, class Emit>
+__device__ __forceinline__ void stream_field(const float *tile, const float *__restrict__ g0,
+                                             const StepArgs &a, int x0, int zw, int lane,
+                                             Emit emit)
+{
+    using S = Shape<MMAX>;
+    constexpr int QN = 2 * MMAX + 1;
+    constexpr int WN = 4 + 2 * S::XH;
+    const int cx = S::XH + 4 * lane;              // smem column of the lane's first cell
+    const int rbase = S::ZH + (zw - (int)(blockIdx.y * TZ)) - MMAX;  // smem row of z-M
+    float4 q[QN];
+#pragma unroll
+    for (int j = 0; j < QN - 1; ++j) q[j] = lds4(tile + (rbase + j) * S::BW + cx);
+#pragma unroll
+    for (int i = 0; i < RW; ++i) {
+        q[QN - 1] = lds4(tile + (rbase + i + QN - 1) * S::BW + cx);
+        const int z = zw + i;
+        if (z < a.NZ) {
+            const float *rowp = tile + (rbase + i + MMAX) * S::BW;
+            float win[WN];
+#pragma unroll
+            for (int j = 0; j < WN / 4; ++j) {
+                float4 t4 = lds4(rowp + 4 * lane + 4 * j);
+                win[4 * j] = t4.x; win[4 * j + 1] = t4.y; win[4 * j + 2] = t4.z; win[4 * j + 3] = t4.w;
+            }
+            const long off = (long)z * a.P + x0 + 4 * lane;
+            const float4 v4 = __ldg(reinterpret_cast<const float4 *>(a.v + off));
+            const float4 u04 = *reinterpret_cast<const float4 *>(g0 + off);
+            float4 res;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float vc = f4get(v4, k);
+                int bin = 0;
+                if (ADAPT) {
+                    bin = (int)((vc - a.vmin) / a.dv + 0.5f);
+                    bin = min(max(bin, 0), a.nbins - 1);
+                }
+                const float *cb = a.ctab + bin;
+                const float u = f4get(q[MMAX], k);
+                float w1 = a.k0 * __ldg(cb) * u;
+#pragma unroll
+                for (int l = 1; l <= MMAX; ++l) {
+                    const float zs = f4get(q[MMAX - l], k) + f4get(q[MMAX + l], k);
+                    const float xs = zs * a.hzx2_1 + win[S::XH + k - l];
+                    w1 = fmaf(__ldg(cb + l * a.nbins), xs + win[S::XH + k + l], w1);
+                }
+                const float vv = vc * vc * a.tao2 * a.h2;
+                f4set(res, k, fmaf(vv, w1, 2.0f * u - f4get(u04, k)));
+            }
+            emit(i, z, off, res);
+        }
+#pragma unroll
+        for (int j = 0; j < QN - 1; ++j) q[j] = q[j + 1];
+    }
+}
+
+template <int MMAX, bool ADAPT, int MODE>
+__global__ void __launch_bounds__(NTHREADS)
+    k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
+           const StepArgs a)
+{
+    using S = Shape<MMAX>;
+    extern __shared__ __align__(128) float smem[];
+    float *tA = smem;
+    float *tS = smem + S::ELEMS;
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(smem + (MODE == MODE_BWD ? 2 : 1) * S::ELEMS);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, S::BYTES * (MODE == MODE_BWD ? 2u : 1u));
+        tma_load_3d(tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, &bar);
+        if (MODE == MODE_BWD) tma_load_3d(tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, &bar);
+    }
+    if (!mbar_wait_bounded(&bar, 0, &g_rtm_dev_error)) {
+        mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
+        return;
+    }
+    patch_halo<MMAX>(tA, x0, z0, a.NX, a.NZ);
+    if (MODE == MODE_BWD) patch_halo<MMAX>(tS, x0, z0, a.NX, a.NZ);
+    __syncthreads();
+
+    const long long so = (long long)shot * a.ss;
+    const int zw = z0 + warp * RW;
+    const int xl = x0 + 4 * lane;
+    const int src = a.src[shot];
+    const int src_z = src / a.NX, src_x = src % a.NX;
+    const int N2 = a.N2, NZ = a.NZ, NX = a.NX;
+
+    // Source field (backward only): interior cells of the warp's rows.
+    float4 sres[RW];
+    if (MODE == MODE_BWD) {
+#pragma unroll
+        for (int i = 0; i < RW; ++i) sres[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool rows_in = (zw + RW > N2) && (zw < NZ - N2);
+        const bool cols_in = (x0 + TX > N2) && (x0 < NX - N2);
+        if (rows_in && cols_in) {
+            stream_field<MMAX, ADAPT>(
+                tS, a.s0 + so, a, x0, zw, lane, [&](int i, int z, long off, float4 r) {
+                    if (z < N2 || z >= NZ - N2) return;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int x = xl + k;
+                        if (x < N2 || x >= NX - N2) {
+                            f4set(r, k, 0.0f);
+                            continue;
+                        }
+                        if (z == src_z && x == src_x) f4set(r, k, f4get(r, k) + a.wavelet);
+                        a.s2[so + off + k] = f4get(r, k);
+                    }
+                    sres[i] = r;
+                });
+        }
+    }
+
+    // Receiver line within this tile?
+    bool line_hit = false;
+    if (a.nrec > 0) {
+        const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = a.rx0 + (a.nrec - 1) * a.rdx;
+        const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(a.rx0, xb), xhi = max(a.rx0, xb);
+        line_hit = !(zhi < z0 || zlo >= z0 + TZ || xhi < x0 || xlo >= x0 + TX);
+    }
+
+    // Field A: u (forward) or R (backward, full grid).
+    stream_field<MMAX, ADAPT>(
+        tA, a.a0 + so, a, x0, zw, lane, [&](int i, int z, long off, float4 r) {
+            const bool zpad = (z < N2 || z >= NZ - N2);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int x = xl + k;
+                float val = f4get(r, k);
+                if (MODE == MODE_FWD && z == src_z && x == src_x) val += a.wavelet;
+                if (MODE == MODE_BWD && line_hit) {
+                    int j = -1;
+                    if (a.rdz == 0) {
+                        if (z == a.rz0 && (x - a.rx0) % a.rdx == 0) j = (x - a.rx0) / a.rdx;
+                    } else if (a.rdx == 0) {
+                        if (x == a.rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
+                    } else if ((x - a.rx0) % a.rdx == 0) {
+                        int jj = (x - a.rx0) / a.rdx;
+                        if (z == a.rz0 + jj * a.rdz) j = jj;
+                    }
+                    if (j >= 0 && j < a.nrec) {
+                        const float d = a.dinj[(long long)shot * a.dstride + j];
+                        if (d != 0.0f) val = d;
+                    }
+                }
+                f4set(r, k, val);
+            }
+            if (!zpad && xl >= N2 && xl + 3 < NX - N2) {
+                *reinterpret_cast<float4 *>(a.a2 + so + off) = r;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int x = xl + k;
+                    if (x >= NX) break;
+                    const bool pad = zpad || x < N2 || x >= NX - N2;
+                    (pad ? a.pre : a.a2)[so + off + k] = f4get(r, k);
+                }
+            }
+            if (MODE == MODE_BWD && !zpad) {
+                // imaging on interior cells (kernel.cu:489-517)
+                const float4 s = sres[i];
+                float4 *p1 = reinterpret_cast<float4 *>(a.rel1 + so + off);
+                float4 *p2 = reinterpret_cast<float4 *>(a.rel2 + so + off);
+                float4 g1 = *p1, g2 = *p2;
+                if (a.compen) {
+                    float4 *ps = reinterpret_cast<float4 *>(a.sacc + so + off);
+                    float4 *pr = reinterpret_cast<float4 *>(a.racc + so + off);
+                    float4 sa = *ps, ra = *pr;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int x = xl + k;
+                        if (x < N2 || x >= NX - N2) continue;
+                        const float sak = f4get(sa, k) + f4get(s, k);
+                        const float rak = f4get(ra, k) + f4get(r, k);
+                        f4set(sa, k, sak);
+                        f4set(ra, k, rak);
+                        f4set(g1, k, f4get(g1, k) + rak * sak);
+                        f4set(g2, k, f4get(g2, k) + f4get(s, k) * f4get(s, k));
+                    }
+                    *ps = sa;
+                    *pr = ra;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int x = xl + k;
+                        if (x < N2 || x >= NX - N2) continue;
+                        f4set(g1, k, f4get(g1, k) + f4get(r, k) * f4get(s, k));
+                        f4set(g2, k, f4get(g2, k) + f4get(s, k) * f4get(s, k));
+                    }
+                }
+                *p1 = g1;
+                *p2 = g2;
+            }
+        });
+}
+
+// ---------------------------------------------------------------------------
+// Pad kernel: one-way update + blend of the absorbing pad (kernel.cu:116-183),
+// ring save / restore, receiver recording.
+
+struct PadArgs {
+    int NZ, NX, P, N2, M, nz, nx, quirk;
+    long long ss;
+    long nabc;
+    float taoh, taoh2;
+    const float *v, *r1, *w;
+    const float *a0, *a1;     // field A levels k-2, k-1
+    float *a2;                // field A level k (interior final, pad written here)
+    const float *pre;         // pre-blend pad values of level k
+    // ring
+    float *ring;              // shot 0, slot k (forward save) or slot k (backward restore)
+    long long ring_ss;        // floats between shots in the ring store
+    int ring_mode;            // 0 none, 1 save a2, 2 restore into s2
+    float *s2;                // backward source field receiving the restore
+    // recording (forward): rec[shot*rec_ss + j] = a1[cell_j]
+    float *rec;
+    long long rec_ss;
+    int rz0, rx0, rdz, rdx, nrec;
+};
+
+__device__ __forceinline__ long ring_index(int z, int x, int NZ, int NX, int N2, int M, int nz,
+                                           int nx)
+{
+    if (x >= N2 && x < NX - N2) {
+        if (z < N2 && z >= N2 - M) return (long)(N2 - 1 - z) * nx + (x - N2);
+        if (z >= NZ - N2 && z < NZ - N2 + M) return (long)M * nx + (long)(z - (NZ - N2)) * nx + (x - N2);
+    }
+    if (z >= N2 && z < NZ - N2) {
+        if (x < N2 && x >= N2 - M) return 2L * M * nx + (long)(N2 - 1 - x) * nz + (z - N2);
+        if (x >= NX - N2 && x < NX - N2 + M)
+            return 2L * M * nx + (long)M * nz + (long)(x - (NX - N2)) * nz + (z - N2);
+    }
+    return -1;
+}
+
+__global__ void __launch_bounds__(256) k_pad(const PadArgs a)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    const long long so = (long long)shot * a.ss;
+    if (t >= a.nabc) {
+        const long j = t - a.nabc;
+        if (a.rec && j < a.nrec) {
+            const int z = a.rz0 + (int)j * a.rdz, x = a.rx0 + (int)j * a.rdx;
+            a.rec[(long long)shot * a.rec_ss + j] = a.a1[so + (long)z * a.P + x];
+        }
+        return;
+    }
+    const AbcCell cc = abc_cell(t, a.NZ, a.NX, a.N2);
+    const int z = cc.z, x = cc.x, NZ = a.NZ, NX = a.NX, N2 = a.N2, P = a.P;
+    const long c = (long)z * P + x;
+    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so, *in2 = a.a2 + so;
+    auto pv = [&](int zz, int xx) -> float {
+        const long i = (long)zz * P + xx;
+        return is_pad(zz, xx, NZ, NX, N2) ? pr[i] : in2[i];
+    };
+    const int ea = min(z, NZ - 1 - z), ee = min(x, NX - 1 - x);
+    const int dz = (z < NZ - 1 - z) ? 1 : -1, dx = (x < NX - 1 - x) ? 1 : -1;
+    float b;
+    if (ee >= ea + 2 || ea >= ee + 2) {
+        int nz_, nx_, sz, sx;
+        long q;  // flat reference index of the lateral-term velocity
+        if (ee >= ea + 2) {
+            nz_ = z + dz; nx_ = x; sz = 0; sx = 1;
+            q = (dz > 0) ? (long)z * NX + x : (long)(NZ - 1 - z) * NX + x;
+        } else {
+            nz_ = z; nx_ = x + dx; sz = 1; sx = 0;
+            q = (dx > 0) ? (long)x * NX + z : (long)(NX - 1 - x) * NX + z;
+        }
+        const float vc = a.v[c];
+        float vq = vc;
+        if (a.quirk) {
+            const int qz = (int)(q / NX), qx = (int)(q % NX);
+            vq = a.v[(long)qz * P + qx];
+        }
+        const long n = (long)nz_ * P + nx_;
+        const float u2n = pv(nz_, nx_);
+        const float lat = pv(nz_ + sz, nx_ + sx) - 2.0f * u2n + pv(nz_ - sz, nx_ - sx) +
+                          u0[(long)(z + sz) * P + x + sx] - 2.0f * u0[c] + u0[(long)(z - sz) * P + x - sx];
+        b = 1.0f / (a.taoh * vc + 1.0f) *
+            (a.taoh * vc * (u2n - u0[n] + u0[c]) - (-2.0f * u1[c] + u0[c] + u2n - 2.0f * u1[n] + u0[n]) +
+             a.taoh2 * vq * vq * lat);
+    } else {
+        const float rr = a.r1[c];
+        b = 1.0f / (2.0f * rr + 1.0f) * (u1[c] + rr * (pv(z, x + dx) + pv(z + dz, x)));
+    }
+    const float wj = a.w[blend_index(z, x, NZ, NX, N2)];
+    const float out = (1.0f - wj) * pr[c] + wj * b;
+    a.a2[so + c] = out;
+    if (a.ring_mode) {
+        const long ri = ring_index(z, x, NZ, NX, N2, a.M, a.nz, a.nx);
+        if (ri >= 0) {
+            if (a.ring_mode == 1)
+                a.ring[(long long)shot * a.ring_ss + ri] = out;
+            else
+                a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + ri];
+        }
+    }
+}
+
+// Ring of one level (used for slot 1 at start-up): ring[ri] = u[cell].
+__global__ void k_ring_fill(const float *__restrict__ u, float *__restrict__ ring, long long ss,
+                            long long ring_ss, int NZ, int NX, int P, int N2, int M)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    if (t >= abc_count(NZ, NX, N2)) return;
+    const AbcCell cc = abc_cell(t, NZ, NX, N2);
+    const long ri = ring_index(cc.z, cc.x, NZ, NX, N2, M, NZ - 2 * N2, NX - 2 * N2);
+    if (ri >= 0) ring[(long long)shot * ring_ss + ri] = u[(long long)shot * ss + (long)cc.z * P + cc.x];
+}
+
+// Start of a shot: u0 = 0, u1 = spike at the source (kernel.cu:798-803).
+__global__ void k_shot_init(float *u0, float *u1, float *u2, float *pre, const int *src,
+                            float spike, long long ss, int NX, int P)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    if (i >= ss) return;
+    const long long o = (long long)shot * ss + i;
+    u0[o] = 0.0f;
+    u2[o] = 0.0f;
+    pre[o] = 0.0f;
+    const int s = src[shot];
+    const long si = (long)(s / NX) * P + s % NX;
+    u1[o] = (i == si) ? spike : 0.0f;
+}
+
+// Hand-off to the backward pass and image initialisation (kernel.cu:822-885).
+// F1 = u_{NT-1}, F0 = u_{NT-2} of the forward run; the host-side forward
+// arrays the reference reads here still hold the initial state (zeros plus
+// the start spike at the source).
+__global__ void k_img_init(const float *F1, const float *F0, float *R0, float *R1, float *R2,
+                           float *rel1, float *rel2, float *sacc, float *racc, const int *src,
+                           float spike, int compen, long long ss, int NX, int P)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    if (i >= ss) return;
+    const long long o = (long long)shot * ss + i;
+    const int s = src[shot];
+    const long si = (long)(s / NX) * P + s % NX;
+    const float h1 = (i == si) ? spike : 0.0f, h0 = 0.0f;
+    const float b0 = F1[o], b1 = F0[o];  // BW0 = u_{NT-1}, BW1 = u_{NT-2}
+    if (compen) {
+        const float bw2 = b0 + b1, fw2 = h0 + h1;
+        rel1[o] = fw2 * bw2 + h0 * b0;
+        rel2[o] = b1 * b1 + b0 * b0;
+        sacc[o] = bw2;
+        racc[o] = fw2;
+    } else {
+        rel1[o] = h1 * b1 + h0 * b0;
+        rel2[o] = b1 * b1 + b0 * b0;
+    }
+    R0[o] = 0.0f;
+    R1[o] = 0.0f;
+    R2[o] = 0.0f;
+}
+
+// Receiver samples of a level (used for the first and last recorded steps).
+__global__ void k_record(const float *u, float *rec, long long ss, long long rec_ss, int P, int rz0,
+                         int rx0, int rdz, int rdx, int nrec)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    if (j >= nrec) return;
+    const int z = rz0 + j * rdz, x = rx0 + j * rdx;
+    rec[(long long)shot * rec_ss + j] = u[(long long)shot * ss + (long)z * P + x];
+}
+
+// ---------------------------------------------------------------------------
+// Per-shot finishing (kernel.cu:935-990) and the compensated stack.
+
+__global__ void k_illum_max(const float *rel2, unsigned *mx, long long ss, int NZ, int NX, int P, int N2)
+{
+    const int shot = blockIdx.y;
+    const int nz = NZ - 2 * N2, nx = NX - 2 * N2;
+    float m = 0.0f;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < (long)nz * nx;
+         t += (long)gridDim.x * blockDim.x) {
+        const int zi = (int)(t / nx), xi = (int)(t % nx);
+        m = fmaxf(m, fabsf(rel2[(long long)shot * ss + (long)(zi + N2) * P + xi + N2]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx + shot, __float_as_uint(m));
+}
+
+// up = -(Laplacian of rel1) * v^2 / vmax^2 with even reflection at the
+// interior edges, down = rel2 + whitecoe*max|rel2|; outputs [shot][nz][nx].
+__global__ void k_finish(const float *rel1, const float *rel2, const float *v, const unsigned *mx,
+                         float *up, float *down, long long ss, int NZ, int NX, int P, int N2,
+                         float vmax, float whitecoe)
+{
+    const int nz = NZ - 2 * N2, nx = NX - 2 * N2;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    if (t >= (long)nz * nx) return;
+    const int zi = (int)(t / nx), xi = (int)(t % nx);
+    const int i = zi + N2, j = xi + N2;
+    int i1 = i - 1, i2 = i + 1, j1 = j - 1, j2 = j + 1;
+    if (i1 < N2) i1 = 2 * N2 - i1;
+    if (j1 < N2) j1 = 2 * N2 - j1;
+    if (i2 >= NZ - N2) i2 = 2 * (NZ - N2 - 1) - i2;
+    if (j2 >= NX - N2) j2 = 2 * (NX - N2 - 1) - j2;
+    const float *g = rel1 + (long long)shot * ss;
+    const float s = g[(long)i * P + j2] + g[(long)i * P + j1] + g[(long)i2 * P + j] +
+                    g[(long)i1 * P + j] - 4.0f * g[(long)i * P + j];
+    const float vv = v[(long)i * P + j];
+    const long long o = (long long)shot * nz * nx + t;
+    up[o] = -1.0f * s * vv * vv / (vmax * vmax);
+    const float stable = __uint_as_float(mx[shot]) * whitecoe;
+    down[o] = rel2[(long long)shot * ss + (long)i * P + j] + stable;
+}
+
+// Compensated (Kahan) accumulation of per-shot images in shot order:
+// sum/comp persist across batches.
+__global__ void k_stack_kahan(const float *up, const float *down, int nshot, long ncell,
+                              float *s1, float *c1, float *s2, float *c2)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) return;
+    float a1 = s1[t], e1 = c1[t], a2 = s2[t], e2 = c2[t];
+    for (int m = 0; m < nshot; ++m) {
+        const float y1 = __fsub_rn(up[(long)m * ncell + t], e1);
+        const float t1 = __fadd_rn(a1, y1);
+        e1 = __fsub_rn(__fsub_rn(t1, a1), y1);
+        a1 = t1;
+        const float y2 = __fsub_rn(down[(long)m * ncell + t], e2);
+        const float t2 = __fadd_rn(a2, y2);
+        e2 = __fsub_rn(__fsub_rn(t2, a2), y2);
+        a2 = t2;
+    }
+    s1[t] = a1; c1[t] = e1; s2[t] = a2; c2[t] = e2;
+}
+
+__global__ void k_stack_final(const float *s1, const float *s2, float *img, float *ill, long ncell,
+                              int nrec, int inorm)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) return;
+    float g1 = s1[t] / (float)nrec, g2 = s2[t] / (float)nrec;
+    if (inorm) g1 = g1 / g2;
+    img[t] = g1;
+    ill[t] = g2;
+}
+
+}  // namespace eng
