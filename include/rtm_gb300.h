@@ -130,6 +130,25 @@ int rtm_prep_wavelet(float *wav, int n, float tao, float f0);
 /* LSMOrCon_rec_2D.cpp:526-551 (order): Taylor coefficients c[0..N/2]. */
 int rtm_prep_taylor(int N, float *c);
 
+/* Least-squares optimiser settings (the reference's parameter file:
+ * nthita, nfdmax, nfdmin, df, eps, fmax; hzx = hz/h). */
+typedef struct rtm_ls_settings {
+    int nthita, nfdmax, nfdmin;
+    double tao, h, df, eps, fmax, hzx;
+} rtm_ls_settings;
+
+/* LSMOrCon_rec_2D.cpp:22-73 (funMandC) in FP64 on the GPU: operator length
+ * len[nvel] (-1 for bins not in need[]), prefix offsets index[nvel+1] and the
+ * float coefficient table coef[index[nvel]] (coef may be NULL to query the
+ * size, returned in *nc).  Bin i is velocity vmin + i*dv. */
+int rtm_coeffs_optimise_fp64(const rtm_ls_settings *s, double vmin, double dv, int nvel,
+                             const int *need, int *len, int *index, float *coef, int ccap,
+                             int *nc);
+/* LSMOrCon_rec_2D.cpp:236-287 (CAL2DFDCOE_LSM) for n cases on the GPU:
+ * c[i*17 + l], l <= M[i] (M[i] <= 16). */
+int rtm_ls_coefs_fp64(const double *r, const double *bb, const int *M, int n, double hzx,
+                      double *c);
+
 /* ======================================================================
  * 3. Shot level.
  * ====================================================================== */

@@ -13,7 +13,9 @@ LIB = os.path.join(LIBDIR, "librtm_gb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
-SOURCES = ["rtm_dropin.cu", "rtm_engine.cu", "rtm_host.cpp"]
+SOURCES = ["rtm_dropin.cu", "rtm_engine.cu", "rtm_host.cpp", "rtm_coeffs.cu"]
+# sources compiled without multiply-add contraction (FP64 parity with the host)
+NOFMA = {"rtm_coeffs.cu"}
 HEADERS = ["rtm_common.cuh", "rtm_engine_kernels.cuh"]
 
 
@@ -25,7 +27,8 @@ def _newest_input() -> float:
 
 def _compile(src: str) -> str:
     out = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
-    cmd = [NVCC, *ARCH, *COMMON, "-c", os.path.join(CSRC, src), "-o", out]
+    extra = ["-fmad=false"] if src in NOFMA else []
+    cmd = [NVCC, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", out]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))

@@ -1,0 +1,42 @@
+"""GPU FP64 least-squares optimiser against the CPU oracle (which is pinned
+bit for bit to the reference's LSMOrCon_rec_2D.cpp).
+
+The GPU solves the same normal equations in the same order; only the
+device's cos/sin/asin may differ from the host's in the last bit, so the
+FP64 coefficients agree to ~1e-9 relative (the LS system is ill conditioned
+at large M) and the float tables agree to a couple of float ulps."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from rtm_gpu_gb300 import coeffs
+from rtm_gpu_gb300.problem import f32
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M", [2, 4, 6, 8, 10])
+def test_single_solves(product_lib, cuda_ok, M):
+    cases = [(0.05, 1.5), (0.2, 2.0), (0.35, 2.5), (0.6, 2.9)]
+    r = np.array([c[0] for c in cases])
+    bb = np.array([c[1] for c in cases])
+    got = coeffs.ls_coefs(r, bb, M)
+    for i, (ri, bi) in enumerate(cases):
+        ref = orc.ls_coefs(ri, bi, M)
+        scale = np.abs(ref).max()
+        assert np.abs(got[i, : M + 1] - ref).max() <= 1e-8 * scale
+
+
+def test_table_matches_oracle(product_lib, cuda_ok):
+    tao, h, fmax, df, nthita, eps = 0.001, 10.0, 50.0, 1.0, 60, 1e-4
+    vmin, dv, nvel = 1500.0, 1.0, 400
+    need = np.ones(nvel, np.int32)
+    need[::7] = 0
+    L, I, C = coeffs.optimise_fp64(nthita=nthita, nfdmax=8, nfdmin=2, tao=tao, h=h, df=df, eps=eps,
+                                   fmax=fmax, hzx=1.0, vmin=vmin, dv=dv, nvel=nvel, need=need)
+    Lo, Io, Co = orc.fun_m_and_c(nthita, 8, 2, nvel, f32(tao), f32(h), df, eps, fmax, vmin, dv,
+                                 need, 1.0)
+    assert np.array_equal(L, Lo)
+    assert np.array_equal(I, Io)
+    ulp = np.spacing(np.abs(Co).astype(np.float32))
+    assert np.all(np.abs(C - Co) <= 4 * ulp)
