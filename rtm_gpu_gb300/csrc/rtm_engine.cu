@@ -72,6 +72,8 @@ struct rtm_ctx {
     int nbins = 1;
     // device
     float *v = nullptr, *r1 = nullptr, *w = nullptr, *ctab = nullptr;
+    int4 *pad_meta = nullptr;
+    float4 *pad_fac = nullptr;
     float *S[3] = {nullptr, nullptr, nullptr}, *R[3] = {nullptr, nullptr, nullptr};
     float *pre = nullptr, *rel1 = nullptr, *rel2 = nullptr, *sacc = nullptr, *racc = nullptr;
     float *ring = nullptr, *data = nullptr, *rec = nullptr, *stage = nullptr;
@@ -120,6 +122,8 @@ void free_all(rtm_ctx *c)
     for (float *p : fl)
         if (p) cudaFree(p);
     if (c->src) cudaFree(c->src);
+    if (c->pad_meta) cudaFree(c->pad_meta);
+    if (c->pad_fac) cudaFree(c->pad_fac);
     if (c->imax) cudaFree(c->imax);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -212,9 +216,9 @@ eng::StepArgs base_step(rtm_ctx *c)
 eng::PadArgs base_pad(rtm_ctx *c)
 {
     eng::PadArgs a{};
-    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2; a.M = c->M; a.nz = c->nz; a.nx = c->nx;
-    a.quirk = c->p.quirk; a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
-    a.taoh = c->p.taoh; a.taoh2 = c->p.taoh2; a.v = c->v; a.r1 = c->r1; a.w = c->w;
+    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2;
+    a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
+    a.meta = c->pad_meta; a.fac = c->pad_fac;
     a.pre = c->pre;
     a.ring_ss = (long long)c->NT * c->ringsz;
     a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = c->nrec;
@@ -545,6 +549,51 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
             cudaMemcpy(c->r1, hr.data(), grid * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(c->w, p->w, (c->N2 + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(c->ctab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+            rtm_set_last_error("upload failed");
+            free_all(c);
+            delete c;
+            return RTM_ERR_CUDA;
+        }
+    }
+    // per-pad-cell classification and model factors (shared by every shot)
+    {
+        const long nabc = abc_count(c->NZ, c->NX, c->N2);
+        std::vector<int4> meta(nabc);
+        std::vector<float4> fac(nabc);
+        const int NZ = c->NZ, NX = c->NX, N2 = c->N2;
+        const float taoh = p->taoh, taoh2 = p->taoh2;
+        for (long t = 0; t < nabc; ++t) {
+            const AbcCell cc = abc_cell(t, NZ, NX, N2);
+            const int z = cc.z, x = cc.x;
+            const int a = std::min(z, NZ - 1 - z), e = std::min(x, NX - 1 - x);
+            const int dz = (z < NZ - 1 - z) ? 1 : -1, dx = (x < NX - 1 - x) ? 1 : -1;
+            int kind;
+            long q = (long)z * NX + x;  // flat index of the lateral-term velocity
+            if (e >= a + 2) {
+                kind = eng::PAD_ROWEDGE;
+                if (p->quirk && dz < 0) q = (long)(NZ - 1 - z) * NX + x;
+            } else if (a >= e + 2) {
+                kind = eng::PAD_COLEDGE;
+                if (p->quirk) q = (dx > 0) ? (long)x * NX + z : (long)(NX - 1 - x) * NX + z;
+            } else {
+                kind = eng::PAD_CORNER;
+            }
+            const long ci = (long)z * NX + x;
+            const float wj = p->w[blend_index(z, x, NZ, NX, N2)];
+            if (kind == eng::PAD_CORNER) {
+                const float rr = p->r1[ci];
+                fac[t] = make_float4(rr, 1.0f / (2.0f * rr + 1.0f), 0.0f, wj);
+            } else {
+                const float vc = p->v[ci], vq = p->v[q];
+                fac[t] = make_float4(taoh * vc, 1.0f / (taoh * vc + 1.0f), taoh2 * vq * vq, wj);
+            }
+            const long ri = c->M > 0 ? eng::ring_index(z, x, NZ, NX, N2, c->M, c->nz, c->nx) : -1;
+            meta[t] = make_int4(z, x, kind | ((dz > 0 ? 1 : 2) << 2) | ((dx > 0 ? 1 : 2) << 4), (int)ri);
+        }
+        TRY(dalloc(c, &c->pad_meta, (size_t)nabc));
+        TRY(dalloc(c, &c->pad_fac, (size_t)nabc));
+        if (cudaMemcpy(c->pad_meta, meta.data(), sizeof(int4) * nabc, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(c->pad_fac, fac.data(), sizeof(float4) * nabc, cudaMemcpyHostToDevice) != cudaSuccess) {
             rtm_set_last_error("upload failed");
             free_all(c);
             delete c;

@@ -330,11 +330,12 @@ __global__ void __launch_bounds__(NTHREADS)
 // ring save / restore, receiver recording.
 
 struct PadArgs {
-    int NZ, NX, P, N2, M, nz, nx, quirk;
+    int NZ, NX, P, N2;
     long long ss;
     long nabc;
-    float taoh, taoh2;
-    const float *v, *r1, *w;
+    const int4 *meta;         // [nabc] {z, x, kind | dz<<2 | dx<<4, ring slot index or -1}
+    const float4 *fac;        // [nabc] side: {taoh*v, 1/(taoh*v+1), taoh2*vq*vq, w}
+                              //        corner: {r_1, 1/(2 r_1+1), 0, w}
     const float *a0, *a1;     // field A levels k-2, k-1
     float *a2;                // field A level k (interior final, pad written here)
     const float *pre;         // pre-blend pad values of level k
@@ -349,8 +350,10 @@ struct PadArgs {
     int rz0, rx0, rdz, rdx, nrec;
 };
 
-__device__ __forceinline__ long ring_index(int z, int x, int NZ, int NX, int N2, int M, int nz,
-                                           int nx)
+enum { PAD_ROWEDGE = 0, PAD_COLEDGE = 1, PAD_CORNER = 2 };
+
+__host__ __device__ __forceinline__ long ring_index(int z, int x, int NZ, int NX, int N2, int M,
+                                                    int nz, int nx)
 {
     if (x >= N2 && x < NX - N2) {
         if (z < N2 && z >= N2 - M) return (long)(N2 - 1 - z) * nx + (x - N2);
@@ -364,6 +367,13 @@ __device__ __forceinline__ long ring_index(int z, int x, int NZ, int NX, int N2,
     return -1;
 }
 
+// One-way update + blend of one pad cell (kernel.cu:116-183).  Side cell c
+// with inward neighbour n and lateral step s:
+//   b = inv*(A*(u2[n]-u0[n]+u0[c]) - (-2u1[c]+u0[c]+u2[n]-2u1[n]+u0[n])
+//           + Q*(u2[n+s]-2u2[n]+u2[n-s]+u0[c+s]-2u0[c]+u0[c-s]))
+// corner: b = inv*(u1[c] + r_1*(u2[c+dx]+u2[c+dz])); u2 is read before
+// blending (pre-blend pad values from `pre`, interior values from a2);
+// out = (1-w)*u2[c] + w*b.
 __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -377,55 +387,41 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         }
         return;
     }
-    const AbcCell cc = abc_cell(t, a.NZ, a.NX, a.N2);
-    const int z = cc.z, x = cc.x, NZ = a.NZ, NX = a.NX, N2 = a.N2, P = a.P;
+    const int4 m = __ldg(a.meta + t);
+    const float4 f = __ldg(a.fac + t);
+    const int z = m.x, x = m.y, kind = m.z & 3;
+    const int dz = ((m.z >> 2) & 3) == 1 ? 1 : -1, dx = ((m.z >> 4) & 3) == 1 ? 1 : -1;
+    const int NZ = a.NZ, NX = a.NX, N2 = a.N2, P = a.P;
     const long c = (long)z * P + x;
     const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so, *in2 = a.a2 + so;
     auto pv = [&](int zz, int xx) -> float {
         const long i = (long)zz * P + xx;
         return is_pad(zz, xx, NZ, NX, N2) ? pr[i] : in2[i];
     };
-    const int ea = min(z, NZ - 1 - z), ee = min(x, NX - 1 - x);
-    const int dz = (z < NZ - 1 - z) ? 1 : -1, dx = (x < NX - 1 - x) ? 1 : -1;
     float b;
-    if (ee >= ea + 2 || ea >= ee + 2) {
+    if (kind != PAD_CORNER) {
         int nz_, nx_, sz, sx;
-        long q;  // flat reference index of the lateral-term velocity
-        if (ee >= ea + 2) {
+        if (kind == PAD_ROWEDGE) {
             nz_ = z + dz; nx_ = x; sz = 0; sx = 1;
-            q = (dz > 0) ? (long)z * NX + x : (long)(NZ - 1 - z) * NX + x;
         } else {
             nz_ = z; nx_ = x + dx; sz = 1; sx = 0;
-            q = (dx > 0) ? (long)x * NX + z : (long)(NX - 1 - x) * NX + z;
-        }
-        const float vc = a.v[c];
-        float vq = vc;
-        if (a.quirk) {
-            const int qz = (int)(q / NX), qx = (int)(q % NX);
-            vq = a.v[(long)qz * P + qx];
         }
         const long n = (long)nz_ * P + nx_;
         const float u2n = pv(nz_, nx_);
         const float lat = pv(nz_ + sz, nx_ + sx) - 2.0f * u2n + pv(nz_ - sz, nx_ - sx) +
                           u0[(long)(z + sz) * P + x + sx] - 2.0f * u0[c] + u0[(long)(z - sz) * P + x - sx];
-        b = 1.0f / (a.taoh * vc + 1.0f) *
-            (a.taoh * vc * (u2n - u0[n] + u0[c]) - (-2.0f * u1[c] + u0[c] + u2n - 2.0f * u1[n] + u0[n]) +
-             a.taoh2 * vq * vq * lat);
+        b = f.y * (f.x * (u2n - u0[n] + u0[c]) - (-2.0f * u1[c] + u0[c] + u2n - 2.0f * u1[n] + u0[n]) +
+                   f.z * lat);
     } else {
-        const float rr = a.r1[c];
-        b = 1.0f / (2.0f * rr + 1.0f) * (u1[c] + rr * (pv(z, x + dx) + pv(z + dz, x)));
+        b = f.y * (u1[c] + f.x * (pv(z, x + dx) + pv(z + dz, x)));
     }
-    const float wj = a.w[blend_index(z, x, NZ, NX, N2)];
-    const float out = (1.0f - wj) * pr[c] + wj * b;
+    const float out = (1.0f - f.w) * pr[c] + f.w * b;
     a.a2[so + c] = out;
-    if (a.ring_mode) {
-        const long ri = ring_index(z, x, NZ, NX, N2, a.M, a.nz, a.nx);
-        if (ri >= 0) {
-            if (a.ring_mode == 1)
-                a.ring[(long long)shot * a.ring_ss + ri] = out;
-            else
-                a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + ri];
-        }
+    if (a.ring_mode && m.w >= 0) {
+        if (a.ring_mode == 1)
+            a.ring[(long long)shot * a.ring_ss + m.w] = out;
+        else
+            a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + m.w];
     }
 }
 
