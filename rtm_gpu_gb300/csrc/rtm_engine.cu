@@ -82,7 +82,10 @@ struct rtm_ctx {
     float *ups = nullptr, *downs = nullptr;                       // per-batch finished images
     float *ks1 = nullptr, *kc1 = nullptr, *ks2 = nullptr, *kc2 = nullptr;  // Kahan state
     float *img = nullptr, *ill = nullptr;
-    CUtensorMap mapS[3], mapR[3];
+    CUtensorMap mapS[3], mapR[3];      // halo boxes of the rotating levels
+    CUtensorMap flatS[3], flatR[3];    // flat tiles of the same buffers
+    CUtensorMap flatV;                 // flat tiles of the model
+    eng::ImgMaps imaps;                // flat tiles of the imaging accumulators
     size_t bytes = 0;
     // graphs keyed by (phase, batch)
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
@@ -136,24 +139,24 @@ void free_all(rtm_ctx *c)
 // ---------------------------------------------------------------------------
 // launch helpers
 
-using StepFn = void (*)(const CUtensorMap, const CUtensorMap, const eng::StepArgs);
+struct StepMaps {
+    const CUtensorMap *A, *S, *A0, *S0;
+};
 
 template <int MMAX, bool AD, int MODE>
-int launch_step_t(rtm_ctx *c, const CUtensorMap &mA, const CUtensorMap &mS,
-                  const eng::StepArgs &a, int nb)
+int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb)
 {
-    using S = eng::Shape<MMAX>;
-    const unsigned smem = S::BYTES * (MODE == eng::MODE_BWD ? 2u : 1u) + 16u;
+    const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
-    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(mA, mS, a);
+    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(*m.A, *m.S, *m.A0, *m.S0,
+                                                                      c->flatV, c->imaps, a);
     return RTM_OK;
 }
 
 template <int MMAX, bool AD, int MODE>
 void set_attr_t()
 {
-    using S = eng::Shape<MMAX>;
-    const int smem = (int)(S::BYTES * (MODE == eng::MODE_BWD ? 2u : 1u) + 16u);
+    const int smem = (int)eng::Smem<MMAX, MODE>::BYTES;
     cudaFuncSetAttribute(eng::k_step<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
@@ -177,24 +180,22 @@ void init_step_attrs()
 }
 
 template <int MMAX>
-int launch_step_m(rtm_ctx *c, int mode, const CUtensorMap &mA, const CUtensorMap &mS,
-                  const eng::StepArgs &a, int nb)
+int launch_step_m(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb)
 {
     const bool ad = c->p.adaptive != 0;
     if (mode == eng::MODE_FWD)
-        return ad ? launch_step_t<MMAX, true, eng::MODE_FWD>(c, mA, mS, a, nb)
-                  : launch_step_t<MMAX, false, eng::MODE_FWD>(c, mA, mS, a, nb);
-    return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, mA, mS, a, nb)
-              : launch_step_t<MMAX, false, eng::MODE_BWD>(c, mA, mS, a, nb);
+        return ad ? launch_step_t<MMAX, true, eng::MODE_FWD>(c, m, a, nb)
+                  : launch_step_t<MMAX, false, eng::MODE_FWD>(c, m, a, nb);
+    return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, m, a, nb)
+              : launch_step_t<MMAX, false, eng::MODE_BWD>(c, m, a, nb);
 }
 
-int launch_step(rtm_ctx *c, int mode, const CUtensorMap &mA, const CUtensorMap &mS,
-                const eng::StepArgs &a, int nb)
+int launch_step(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb)
 {
     switch (c->MM) {
-    case 4: return launch_step_m<4>(c, mode, mA, mS, a, nb);
-    case 8: return launch_step_m<8>(c, mode, mA, mS, a, nb);
-    case 12: return launch_step_m<12>(c, mode, mA, mS, a, nb);
+    case 4: return launch_step_m<4>(c, mode, m, a, nb);
+    case 8: return launch_step_m<8>(c, mode, m, a, nb);
+    case 12: return launch_step_m<12>(c, mode, m, a, nb);
     default: rtm_set_last_error("unsupported operator length"); return RTM_ERR_UNSUPPORTED;
     }
 }
@@ -271,8 +272,9 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         sa.a0 = a0; sa.a2 = a2; sa.pre = c->pre;
         sa.wavelet = (k < c->p.NT2) ? c->wav[k - 1] : 0.0f;
         tic(c);
-        if (int rc = launch_step(c, eng::MODE_FWD, c->mapS[(k - 1) % 3], c->mapS[(k - 1) % 3], sa, nb))
-            return rc;
+        const StepMaps sm{&c->mapS[(k - 1) % 3], &c->mapS[(k - 1) % 3], &c->flatS[(k - 2) % 3],
+                          &c->flatS[(k - 2) % 3]};
+        if (int rc = launch_step(c, eng::MODE_FWD, sm, sa, nb)) return rc;
         toc(c, 0);
         pa.a0 = a0; pa.a1 = a1; pa.a2 = a2;
         pa.ring_mode = c->M > 0 ? 1 : 0;
@@ -316,7 +318,8 @@ int enqueue_backward(rtm_ctx *c, int nb)
         sa.wavelet = (k < c->p.NT2) ? c->wav[k + 1] : 0.0f;
         sa.dinj = c->data + (long long)(k + 1) * c->nrec;
         tic(c);
-        if (int rc = launch_step(c, eng::MODE_BWD, c->mapR[i1], c->mapS[i1], sa, nb)) return rc;
+        const StepMaps sm{&c->mapR[i1], &c->mapS[i1], &c->flatR[i0], &c->flatS[i0]};
+        if (int rc = launch_step(c, eng::MODE_BWD, sm, sa, nb)) return rc;
         toc(c, 1);
         pa.a0 = c->R[i0]; pa.a1 = c->R[i1]; pa.a2 = c->R[i2];
         pa.ring_mode = c->M > 0 ? 2 : 0;
@@ -609,7 +612,14 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     for (int i = 0; i < 3; ++i) {
         TRY(make_map(&c->mapS[i], c->S[i], c->NX, c->NZ, c->B, c->P, bw, bh));
         TRY(make_map(&c->mapR[i], c->R[i], c->NX, c->NZ, c->B, c->P, bw, bh));
+        TRY(make_map(&c->flatS[i], c->S[i], c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
+        TRY(make_map(&c->flatR[i], c->R[i], c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
     }
+    TRY(make_map(&c->flatV, c->v, c->NX, c->NZ, 1, c->P, eng::TX, eng::TZ));
+    TRY(make_map(&c->imaps.rel1, c->rel1, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
+    TRY(make_map(&c->imaps.rel2, c->rel2, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
+    TRY(make_map(&c->imaps.sacc, c->sacc, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
+    TRY(make_map(&c->imaps.racc, c->racc, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
 #undef TRY
     cudaEventCreate(&c->ev[0]);
     cudaEventCreate(&c->ev[1]);

@@ -34,11 +34,14 @@ __device__ unsigned int g_rtm_dev_error = 0;
 
 namespace eng {
 
-constexpr int TX = 128;             // tile width: 32 lanes x 4 cells
-constexpr int WARPS = 4;            // warps per CTA
-constexpr int RW = 8;               // rows per warp (z streaming length)
-constexpr int TZ = WARPS * RW;      // tile height
-constexpr int NTHREADS = WARPS * 32;
+constexpr int WX = 4;               // warps across a tile (one column per lane)
+constexpr int WZ = 2;               // warps down a tile
+constexpr int RW = 8;               // rows streamed by one warp
+constexpr int TX = WX * 32;         // tile width (128 columns)
+constexpr int TZ = WZ * RW;         // tile height (16 rows)
+constexpr int NTHREADS = WX * WZ * 32;
+constexpr int FLAT = TX * TZ;       // floats of one flat (halo-free) tile
+constexpr unsigned FLAT_BYTES = FLAT * 4u;
 
 template <int MMAX>
 struct Shape {
@@ -48,6 +51,20 @@ struct Shape {
     static constexpr int BH = TZ + 2 * ZH;         // box height (rows)
     static constexpr int ELEMS = BW * BH;
     static constexpr unsigned BYTES = ELEMS * 4u;
+};
+
+// Shared-memory plan of k_step: halo boxes of the field(s) being advanced,
+// then flat tiles (u_{k-2} of each field, v, and the four imaging
+// accumulators in the backward step), then the mbarrier.
+template <int MMAX, int MODE>
+struct Smem {
+    static constexpr int NBOX = MODE == 1 ? 2 : 1;
+    static constexpr int NFLAT = MODE == 1 ? 7 : 2;  // fwd: a0, v; bwd: a0, s0, v, rel1, rel2, sacc, racc
+    static constexpr unsigned BYTES = NBOX * Shape<MMAX>::BYTES + NFLAT * FLAT_BYTES + 16u;
+};
+
+struct ImgMaps {
+    CUtensorMap rel1, rel2, sacc, racc;
 };
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
@@ -109,86 +126,72 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
     }
 }
 
-__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
-__device__ __forceinline__ float f4get(const float4 &v, int k)
-{
-    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
-}
-__device__ __forceinline__ void f4set(float4 &v, int k, float a)
-{
-    if (k == 0) v.x = a; else if (k == 1) v.y = a; else if (k == 2) v.z = a; else v.w = a;
-}
-
-// Stream one field over the warp's RW rows.  For each row with z < NZ, the
-// lane's 4 cells get u2 = 2u1 - u0 + v^2 tao^2/h^2 * L(u1) and `emit` is
-// called with the results.  `q` is the register queue of rows z-M .. z+M.
+// Stream one field down the warp's RW rows at the lane's column.  For each
+// row z < NZ the cell gets u2 = 2u1 - u0 + v^2 tao^2/h^2 * L(u1) and `emit`
+// is called with the result.  q is the register queue of the column's rows
+// z-M .. z+M; x-neighbours come from the staged halo box, u0 and v from the
+// staged flat tiles (row i at fr + i*TX).
 template <int MMAX, bool ADAPT, class Emit>
-__device__ __forceinline__ void stream_field(const float *tile, const float *__restrict__ g0,
-                                             const StepArgs &a, int x0, int zw, int lane,
+__device__ __forceinline__ void stream_field(const float *box, const float *f0, const float *fv,
+                                             const StepArgs &a, int zw, int rbase, int cx, int fr,
                                              Emit emit)
 {
     using S = Shape<MMAX>;
     constexpr int QN = 2 * MMAX + 1;
-    constexpr int WN = 4 + 2 * S::XH;
-    const int cx = S::XH + 4 * lane;              // smem column of the lane's first cell
-    const int rbase = S::ZH + (zw - (int)(blockIdx.y * TZ)) - MMAX;  // smem row of z-M
-    float4 q[QN];
+    float q[QN];
 #pragma unroll
-    for (int j = 0; j < QN - 1; ++j) q[j] = lds4(tile + (rbase + j) * S::BW + cx);
+    for (int j = 0; j < QN - 1; ++j) q[j] = box[(rbase + j) * S::BW + cx];
 #pragma unroll
     for (int i = 0; i < RW; ++i) {
-        q[QN - 1] = lds4(tile + (rbase + i + QN - 1) * S::BW + cx);
+        q[QN - 1] = box[(rbase + i + QN - 1) * S::BW + cx];
         const int z = zw + i;
         if (z < a.NZ) {
-            const float *rowp = tile + (rbase + i + MMAX) * S::BW;
-            float win[WN];
-#pragma unroll
-            for (int j = 0; j < WN / 4; ++j) {
-                float4 t4 = lds4(rowp + 4 * lane + 4 * j);
-                win[4 * j] = t4.x; win[4 * j + 1] = t4.y; win[4 * j + 2] = t4.z; win[4 * j + 3] = t4.w;
+            const float *rowp = box + (rbase + i + MMAX) * S::BW + cx;
+            const float vc = fv[fr + i * TX];
+            const float u0 = f0[fr + i * TX];
+            int bin = 0;
+            if (ADAPT) {
+                bin = (int)((vc - a.vmin) / a.dv + 0.5f);
+                bin = min(max(bin, 0), a.nbins - 1);
             }
-            const long off = (long)z * a.P + x0 + 4 * lane;
-            const float4 v4 = __ldg(reinterpret_cast<const float4 *>(a.v + off));
-            const float4 u04 = *reinterpret_cast<const float4 *>(g0 + off);
-            float4 res;
+            const float *cb = a.ctab + bin;
+            const float u = q[MMAX];
+            float w1 = a.k0 * __ldg(cb) * u;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float vc = f4get(v4, k);
-                int bin = 0;
-                if (ADAPT) {
-                    bin = (int)((vc - a.vmin) / a.dv + 0.5f);
-                    bin = min(max(bin, 0), a.nbins - 1);
-                }
-                const float *cb = a.ctab + bin;
-                const float u = f4get(q[MMAX], k);
-                float w1 = a.k0 * __ldg(cb) * u;
-#pragma unroll
-                for (int l = 1; l <= MMAX; ++l) {
-                    const float zs = f4get(q[MMAX - l], k) + f4get(q[MMAX + l], k);
-                    const float xs = zs * a.hzx2_1 + win[S::XH + k - l];
-                    w1 = fmaf(__ldg(cb + l * a.nbins), xs + win[S::XH + k + l], w1);
-                }
-                const float vv = vc * vc * a.tao2 * a.h2;
-                f4set(res, k, fmaf(vv, w1, 2.0f * u - f4get(u04, k)));
+            for (int l = 1; l <= MMAX; ++l) {
+                const float xs = (q[MMAX - l] + q[MMAX + l]) * a.hzx2_1 + rowp[-l];
+                w1 = fmaf(__ldg(cb + l * a.nbins), xs + rowp[l], w1);
             }
-            emit(i, z, off, res);
+            const float vv = vc * vc * a.tao2 * a.h2;
+            emit(i, z, fmaf(vv, w1, 2.0f * u - u0));
         }
 #pragma unroll
         for (int j = 0; j < QN - 1; ++j) q[j] = q[j + 1];
     }
 }
 
+// One time step of a batch of shots on one 128 x 16 tile (grid: tiles x
+// tiles x shots).  All inputs arrive by TMA into shared memory under one
+// mbarrier; outputs are stored directly.
 template <int MMAX, bool ADAPT, int MODE>
 __global__ void __launch_bounds__(NTHREADS)
     k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
+           const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
+           const __grid_constant__ CUtensorMap flatV, const __grid_constant__ ImgMaps img,
            const StepArgs a)
 {
     using S = Shape<MMAX>;
+    using SM = Smem<MMAX, MODE>;
     extern __shared__ __align__(128) float smem[];
     float *tA = smem;
-    float *tS = smem + S::ELEMS;
-    uint64_t &bar = *reinterpret_cast<uint64_t *>(smem + (MODE == MODE_BWD ? 2 : 1) * S::ELEMS);
+    float *tS = smem + S::ELEMS;                          // backward only
+    float *fl = smem + SM::NBOX * S::ELEMS;               // flat tiles
+    float *fA0 = fl, *fV = fl + FLAT;
+    float *fS0 = fl + 2 * FLAT, *fR1 = fl + 3 * FLAT, *fR2 = fl + 4 * FLAT;
+    float *fSa = fl + 5 * FLAT, *fRa = fl + 6 * FLAT;
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(fl + SM::NFLAT * FLAT);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wx = warp % WX, wz = warp / WX;
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z;
 
     if (threadIdx.x == 0) {
@@ -197,9 +200,18 @@ __global__ void __launch_bounds__(NTHREADS)
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, S::BYTES * (MODE == MODE_BWD ? 2u : 1u));
+        mbar_arrive_expect_tx(&bar, SM::BYTES - 16u);
         tma_load_3d(tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, &bar);
-        if (MODE == MODE_BWD) tma_load_3d(tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, &bar);
+        tma_load_3d(fA0, &flatA0, x0, z0, shot, &bar);
+        tma_load_3d(fV, &flatV, x0, z0, 0, &bar);
+        if (MODE == MODE_BWD) {
+            tma_load_3d(tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, &bar);
+            tma_load_3d(fS0, &flatS0, x0, z0, shot, &bar);
+            tma_load_3d(fR1, &img.rel1, x0, z0, shot, &bar);
+            tma_load_3d(fR2, &img.rel2, x0, z0, shot, &bar);
+            tma_load_3d(fSa, &img.sacc, x0, z0, shot, &bar);
+            tma_load_3d(fRa, &img.racc, x0, z0, shot, &bar);
+        }
     }
     if (!mbar_wait_bounded(&bar, 0, &g_rtm_dev_error)) {
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
@@ -210,117 +222,81 @@ __global__ void __launch_bounds__(NTHREADS)
     __syncthreads();
 
     const long long so = (long long)shot * a.ss;
-    const int zw = z0 + warp * RW;
-    const int xl = x0 + 4 * lane;
+    const int zw = z0 + wz * RW;             // first row of this warp
+    const int gx = x0 + wx * 32 + lane;      // this lane's column
+    const int cx = S::XH + wx * 32 + lane;   // its column in the halo box
+    const int rbase = wz * RW;               // box row of zw - MMAX
+    const int fr = wz * RW * TX + wx * 32 + lane;  // flat-tile index of row zw
     const int src = a.src[shot];
     const int src_z = src / a.NX, src_x = src % a.NX;
     const int N2 = a.N2, NZ = a.NZ, NX = a.NX;
+    const bool col_in = gx >= N2 && gx < NX - N2;
+    const bool col_ok = gx < NX;
+    const long goff0 = (long)zw * a.P + gx;  // global index of row zw
 
-    // Source field (backward only): interior cells of the warp's rows.
-    float4 sres[RW];
+    // Source field (backward only): interior cells.
+    float sres[RW];
     if (MODE == MODE_BWD) {
 #pragma unroll
-        for (int i = 0; i < RW; ++i) sres[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = 0; i < RW; ++i) sres[i] = 0.0f;
         const bool rows_in = (zw + RW > N2) && (zw < NZ - N2);
-        const bool cols_in = (x0 + TX > N2) && (x0 < NX - N2);
+        const bool cols_in = (x0 + wx * 32 + 32 > N2) && (x0 + wx * 32 < NX - N2);
         if (rows_in && cols_in) {
-            stream_field<MMAX, ADAPT>(
-                tS, a.s0 + so, a, x0, zw, lane, [&](int i, int z, long off, float4 r) {
-                    if (z < N2 || z >= NZ - N2) return;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int x = xl + k;
-                        if (x < N2 || x >= NX - N2) {
-                            f4set(r, k, 0.0f);
-                            continue;
-                        }
-                        if (z == src_z && x == src_x) f4set(r, k, f4get(r, k) + a.wavelet);
-                        a.s2[so + off + k] = f4get(r, k);
-                    }
-                    sres[i] = r;
-                });
+            stream_field<MMAX, ADAPT>(tS, fS0, fV, a, zw, rbase, cx, fr,
+                                      [&](int i, int z, float r) {
+                                          if (z < N2 || z >= NZ - N2 || !col_in) return;
+                                          if (z == src_z && gx == src_x) r += a.wavelet;
+                                          a.s2[so + goff0 + (long)i * a.P] = r;
+                                          sres[i] = r;
+                                      });
         }
     }
 
-    // Receiver line within this tile?
+    // Receiver line within this warp's strip?
     bool line_hit = false;
-    if (a.nrec > 0) {
+    if (MODE == MODE_BWD && a.nrec > 0) {
         const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = a.rx0 + (a.nrec - 1) * a.rdx;
         const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(a.rx0, xb), xhi = max(a.rx0, xb);
-        line_hit = !(zhi < z0 || zlo >= z0 + TZ || xhi < x0 || xlo >= x0 + TX);
+        line_hit = !(zhi < zw || zlo >= zw + RW || xhi < x0 + wx * 32 || xlo >= x0 + wx * 32 + 32);
     }
 
     // Field A: u (forward) or R (backward, full grid).
     stream_field<MMAX, ADAPT>(
-        tA, a.a0 + so, a, x0, zw, lane, [&](int i, int z, long off, float4 r) {
-            const bool zpad = (z < N2 || z >= NZ - N2);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int x = xl + k;
-                float val = f4get(r, k);
-                if (MODE == MODE_FWD && z == src_z && x == src_x) val += a.wavelet;
-                if (MODE == MODE_BWD && line_hit) {
-                    int j = -1;
-                    if (a.rdz == 0) {
-                        if (z == a.rz0 && (x - a.rx0) % a.rdx == 0) j = (x - a.rx0) / a.rdx;
-                    } else if (a.rdx == 0) {
-                        if (x == a.rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
-                    } else if ((x - a.rx0) % a.rdx == 0) {
-                        int jj = (x - a.rx0) / a.rdx;
-                        if (z == a.rz0 + jj * a.rdz) j = jj;
-                    }
-                    if (j >= 0 && j < a.nrec) {
-                        const float d = a.dinj[(long long)shot * a.dstride + j];
-                        if (d != 0.0f) val = d;
-                    }
+        tA, fA0, fV, a, zw, rbase, cx, fr, [&](int i, int z, float val) {
+            if (!col_ok) return;
+            if (MODE == MODE_FWD && z == src_z && gx == src_x) val += a.wavelet;
+            if (MODE == MODE_BWD && line_hit) {
+                int j = -1;
+                if (a.rdz == 0) {
+                    if (z == a.rz0 && (gx - a.rx0) % a.rdx == 0) j = (gx - a.rx0) / a.rdx;
+                } else if (a.rdx == 0) {
+                    if (gx == a.rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
+                } else if ((gx - a.rx0) % a.rdx == 0) {
+                    const int jj = (gx - a.rx0) / a.rdx;
+                    if (z == a.rz0 + jj * a.rdz) j = jj;
                 }
-                f4set(r, k, val);
-            }
-            if (!zpad && xl >= N2 && xl + 3 < NX - N2) {
-                *reinterpret_cast<float4 *>(a.a2 + so + off) = r;
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int x = xl + k;
-                    if (x >= NX) break;
-                    const bool pad = zpad || x < N2 || x >= NX - N2;
-                    (pad ? a.pre : a.a2)[so + off + k] = f4get(r, k);
+                if (j >= 0 && j < a.nrec) {
+                    const float d = a.dinj[(long long)shot * a.dstride + j];
+                    if (d != 0.0f) val = d;
                 }
             }
-            if (MODE == MODE_BWD && !zpad) {
-                // imaging on interior cells (kernel.cu:489-517)
-                const float4 s = sres[i];
-                float4 *p1 = reinterpret_cast<float4 *>(a.rel1 + so + off);
-                float4 *p2 = reinterpret_cast<float4 *>(a.rel2 + so + off);
-                float4 g1 = *p1, g2 = *p2;
+            const bool interior = col_in && z >= N2 && z < NZ - N2;
+            const long long g = so + goff0 + (long)i * a.P;
+            (interior ? a.a2 : a.pre)[g] = val;
+            if (MODE == MODE_BWD && interior) {
+                // imaging (kernel.cu:489-517)
+                const int t = fr + i * TX;
+                const float sv = sres[i];
                 if (a.compen) {
-                    float4 *ps = reinterpret_cast<float4 *>(a.sacc + so + off);
-                    float4 *pr = reinterpret_cast<float4 *>(a.racc + so + off);
-                    float4 sa = *ps, ra = *pr;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int x = xl + k;
-                        if (x < N2 || x >= NX - N2) continue;
-                        const float sak = f4get(sa, k) + f4get(s, k);
-                        const float rak = f4get(ra, k) + f4get(r, k);
-                        f4set(sa, k, sak);
-                        f4set(ra, k, rak);
-                        f4set(g1, k, f4get(g1, k) + rak * sak);
-                        f4set(g2, k, f4get(g2, k) + f4get(s, k) * f4get(s, k));
-                    }
-                    *ps = sa;
-                    *pr = ra;
+                    const float sa = fSa[t] + sv;
+                    const float ra = fRa[t] + val;
+                    a.sacc[g] = sa;
+                    a.racc[g] = ra;
+                    a.rel1[g] = fR1[t] + ra * sa;
                 } else {
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int x = xl + k;
-                        if (x < N2 || x >= NX - N2) continue;
-                        f4set(g1, k, f4get(g1, k) + f4get(r, k) * f4get(s, k));
-                        f4set(g2, k, f4get(g2, k) + f4get(s, k) * f4get(s, k));
-                    }
+                    a.rel1[g] = fR1[t] + val * sv;
                 }
-                *p1 = g1;
-                *p2 = g2;
+                a.rel2[g] = fR2[t] + sv * sv;
             }
         });
 }
