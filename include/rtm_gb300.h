@@ -111,6 +111,17 @@ int rtm_k_Rel_NonCompen(float *DBW2, float *DFW2, float *Drel1, float *Drel2, in
 int rtm_k_Rel_Compen(float *DBW2, float *DFW2, float *DBWADD, float *DFWADD, float *Drel1,
                      float *Drel2, int NZ, int NX, rtm_stream_t s);
 
+/* No counterpart in the reference.  The same update as rtm_k_Hybrid1 followed
+ * by rtm_k_Hybrid2 (or the BK pair), for callers that cannot allocate device
+ * memory where they step the wavefield (their device memory belongs to their
+ * own pool, or their time loop must not call cudaMalloc): the one-way scratch
+ * lives in a fixed 1,048,576-value device array inside this library instead of
+ * a caller DFWb buffer.  Pads with more cells are rejected (RTM_ERR_ARG).  All
+ * calls share that array, so calls overlapping on the GPU race; the first call
+ * on each device looks the array up (before any stream capture, please). */
+int rtm_k_HybridStatic(float *DFW1, float *DFW0, float *DFW2, float *Dv, float *Dr_1, float *Dw,
+                       int NZ, int NX, int N2, float taoh, float taoh2, rtm_stream_t s);
+
 /* ======================================================================
  * 2. Host preparation (replaces the reference's host set-up code).
  * ====================================================================== */
