@@ -77,6 +77,10 @@ struct rtm_ctx {
     float *S[3] = {nullptr, nullptr, nullptr}, *R[3] = {nullptr, nullptr, nullptr};
     float *pre = nullptr, *rel1 = nullptr, *rel2 = nullptr, *sacc = nullptr, *racc = nullptr;
     float *ring = nullptr, *data = nullptr, *rec = nullptr, *stage = nullptr;
+    // 16-bit ring store (ring_precision BF16 / F16)
+    uint16_t *ring16 = nullptr;
+    float *rstage = nullptr, *rscale = nullptr;  // [2][B][ringsz], [B][NT]
+    unsigned *ramax = nullptr;                    // [B][NT]
     int *src = nullptr;
     unsigned *imax = nullptr;
     float *ups = nullptr, *downs = nullptr;                       // per-batch finished images
@@ -125,6 +129,10 @@ void free_all(rtm_ctx *c)
     for (float *p : fl)
         if (p) cudaFree(p);
     if (c->src) cudaFree(c->src);
+    if (c->ring16) cudaFree(c->ring16);
+    if (c->rstage) cudaFree(c->rstage);
+    if (c->rscale) cudaFree(c->rscale);
+    if (c->ramax) cudaFree(c->ramax);
     if (c->pad_meta) cudaFree(c->pad_meta);
     if (c->pad_fac) cudaFree(c->pad_fac);
     if (c->imax) cudaFree(c->imax);
@@ -221,6 +229,13 @@ eng::PadArgs base_pad(rtm_ctx *c)
     a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
     a.meta = c->pad_meta; a.fac = c->pad_fac;
     a.pre = c->pre;
+    a.ring_prec = c->p.ring_precision;
+    a.ringsz = c->ringsz;
+    a.slots = c->NT;
+    a.ring16 = c->ring16;
+    a.amax = c->ramax;
+    a.scale = c->rscale;
+    a.qslot = -1;
     a.ring_ss = (long long)c->NT * c->ringsz;
     a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = c->nrec;
     return a;
@@ -253,9 +268,20 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     eng::k_shot_init<<<dim3(cdiv(ss, 256), nb), 256, 0, c->st>>>(c->S[0], c->S[1], c->S[2], c->pre,
                                                                  c->src, c->p.spike, ss, c->NX, c->P);
     c->launches++;
-    if (c->M > 0)
-        eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
-            c->S[1], c->ring + c->ringsz, ss, (long long)NT * c->ringsz, c->NZ, c->NX, c->P, c->N2, c->M);
+    const bool r16 = c->p.ring_precision != RTM_RING_F32;
+    const long long bstage = (long long)c->B * c->ringsz;  // floats of one stage parity
+    if (r16 && c->M > 0)
+        RTM_CUDA_TRY(cudaMemsetAsync(c->ramax, 0, sizeof(unsigned) * (size_t)c->B * NT, c->st));
+    if (c->M > 0) {
+        if (r16)
+            eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
+                c->S[1], c->rstage + 1 * bstage, ss, c->ringsz, c->NZ, c->NX, c->P, c->N2, c->M,
+                c->ramax + 1, NT);
+        else
+            eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
+                c->S[1], c->ring + c->ringsz, ss, (long long)NT * c->ringsz, c->NZ, c->NX, c->P, c->N2,
+                c->M, nullptr, 0);
+    }
     c->launches += (c->M > 0);
     const long long rss = (long long)NT * c->nrec;
     if (rec_on && c->nrec > 0) {
@@ -266,7 +292,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     RTM_LAUNCH_CHECK();
     eng::StepArgs sa = base_step(c);
     eng::PadArgs pa = base_pad(c);
-    const long npad = abc_count(c->NZ, c->NX, c->N2) + (rec_on ? c->nrec : 0);
+    const long npad = abc_count(c->NZ, c->NX, c->N2) + (rec_on ? c->nrec : 0) + (r16 ? c->ringsz : 0);
     for (int k = 2; k < NT; ++k) {
         float *a0 = c->S[(k - 2) % 3], *a1 = c->S[(k - 1) % 3], *a2 = c->S[k % 3];
         sa.a0 = a0; sa.a2 = a2; sa.pre = c->pre;
@@ -278,7 +304,13 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         toc(c, 0);
         pa.a0 = a0; pa.a1 = a1; pa.a2 = a2;
         pa.ring_mode = c->M > 0 ? 1 : 0;
-        pa.ring = c->ring + (long long)k * c->ringsz;
+        pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
+        if (r16) {
+            pa.slot = k;
+            pa.qslot = k - 1;
+            pa.stage = c->rstage + (k & 1) * bstage;
+            pa.qstage = c->rstage + ((k - 1) & 1) * bstage;
+        }
         pa.rec = rec_on ? c->rec + (long long)(k - 1) * c->nrec : nullptr;
         pa.rec_ss = rss;
         tic(c);
@@ -323,7 +355,8 @@ int enqueue_backward(rtm_ctx *c, int nb)
         toc(c, 1);
         pa.a0 = c->R[i0]; pa.a1 = c->R[i1]; pa.a2 = c->R[i2];
         pa.ring_mode = c->M > 0 ? 2 : 0;
-        pa.ring = c->ring + (long long)k * c->ringsz;
+        pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
+        pa.slot = k;
         pa.s2 = c->S[i2];
         pa.rec = nullptr;
         tic(c);
@@ -436,7 +469,7 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     *out = nullptr;
     if (p->nz < 1 || p->nx < 1 || p->N2 < 2 || p->M < 0 || p->M > p->N2 || p->NT < 4 || !p->v ||
         !p->r1 || !p->w || !p->coef || !p->wav || (p->adaptive && (!p->index || p->nbins < 1)) ||
-        p->ring_precision != RTM_RING_F32) {
+        p->ring_precision < RTM_RING_F32 || p->ring_precision > RTM_RING_F16) {
         rtm_set_last_error("rtm_ctx_create: invalid problem");
         return RTM_ERR_ARG;
     }
@@ -525,7 +558,14 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     TRY(dalloc(c, &c->rel2, bgrid));
     TRY(dalloc(c, &c->sacc, bgrid));
     TRY(dalloc(c, &c->racc, bgrid));
-    TRY(dalloc(c, &c->ring, (size_t)c->B * c->NT * std::max<long>(c->ringsz, 1)));
+    if (p->ring_precision == RTM_RING_F32) {
+        TRY(dalloc(c, &c->ring, (size_t)c->B * c->NT * std::max<long>(c->ringsz, 1)));
+    } else {
+        TRY(dalloc(c, &c->ring16, (size_t)c->B * c->NT * std::max<long>(c->ringsz, 1)));
+        TRY(dalloc(c, &c->rstage, (size_t)2 * c->B * std::max<long>(c->ringsz, 1)));
+        TRY(dalloc(c, &c->rscale, (size_t)c->B * c->NT));
+        TRY(dalloc(c, &c->ramax, (size_t)c->B * c->NT));
+    }
     TRY(dalloc(c, &c->data, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
     TRY(dalloc(c, &c->rec, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
     TRY(dalloc(c, &c->stage, (size_t)c->B * c->NT * std::max(c->nrec, 1)));

@@ -26,6 +26,9 @@
 //             source field (backward), receiver recording (forward).
 #pragma once
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "rtm_common.cuh"
 
 // Device-side error word of the engine (zero = fine); read and cleared by
@@ -324,7 +327,36 @@ struct PadArgs {
     float *rec;
     long long rec_ss;
     int rz0, rx0, rdz, rdx, nrec;
+    // 16-bit ring store (ring_prec 1: bf16, 2: fp16) with per-step max-abs
+    // scaling.  Forward: the blended ring values of step k go to the FP32
+    // stage (stage + shot*ringsz) and their max |value| to amax[shot][k];
+    // the quantisation of slot qslot (= k-1, whose max is final by now) from
+    // qstage runs on extra threads of the same launch.  Backward: slot k is
+    // read back as q * scale[shot][k].
+    int ring_prec;
+    long ringsz;
+    long long slots;         // NT: slots per shot in ring16 / amax / scale
+    uint16_t *ring16;        // [shot][NT][ringsz]
+    float *stage;            // FP32 values of this step   [shot][ringsz]
+    const float *qstage;     // FP32 values of slot qslot  [shot][ringsz]
+    unsigned *amax;          // [shot][NT] float bits of max |value|
+    float *scale;            // [shot][NT] dequantisation factor
+    int slot, qslot;         // slot written (fwd) / restored (bwd); slot to quantise (<0: none)
 };
+
+constexpr float RING16_TARGET = 16384.0f;  // max |value| maps here (fp16 max is 65504)
+
+__device__ __forceinline__ uint16_t ring_quant(float v, float inv, int prec)
+{
+    if (prec == 1) return __bfloat16_as_ushort(__float2bfloat16_rn(v * inv));
+    return __half_as_ushort(__float2half_rn(v * inv));
+}
+
+__device__ __forceinline__ float ring_dequant(uint16_t q, float sc, int prec)
+{
+    const float f = prec == 1 ? __bfloat162float(__ushort_as_bfloat16(q)) : __half2float(__ushort_as_half(q));
+    return f * sc;
+}
 
 enum { PAD_ROWEDGE = 0, PAD_COLEDGE = 1, PAD_CORNER = 2 };
 
@@ -356,10 +388,19 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
     const int shot = blockIdx.y;
     const long long so = (long long)shot * a.ss;
     if (t >= a.nabc) {
-        const long j = t - a.nabc;
+        long j = t - a.nabc;
         if (a.rec && j < a.nrec) {
             const int z = a.rz0 + (int)j * a.rdz, x = a.rx0 + (int)j * a.rdx;
             a.rec[(long long)shot * a.rec_ss + j] = a.a1[so + (long)z * a.P + x];
+            return;
+        }
+        if (a.rec) j -= a.nrec;
+        if (a.ring_prec && a.ring_mode == 1 && a.qslot >= 0 && j < a.ringsz) {
+            const long long sl = (long long)shot * a.slots + a.qslot;
+            const float mx = __uint_as_float(a.amax[sl]);
+            const float inv = mx > 0.0f ? RING16_TARGET / mx : 0.0f;
+            a.ring16[sl * a.ringsz + j] = ring_quant(a.qstage[(long long)shot * a.ringsz + j], inv, a.ring_prec);
+            if (j == 0) a.scale[sl] = mx / RING16_TARGET;
         }
         return;
     }
@@ -394,23 +435,37 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
     const float out = (1.0f - f.w) * pr[c] + f.w * b;
     a.a2[so + c] = out;
     if (a.ring_mode && m.w >= 0) {
-        if (a.ring_mode == 1)
-            a.ring[(long long)shot * a.ring_ss + m.w] = out;
-        else
-            a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + m.w];
+        if (a.ring_prec == 0) {
+            if (a.ring_mode == 1)
+                a.ring[(long long)shot * a.ring_ss + m.w] = out;
+            else
+                a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + m.w];
+        } else if (a.ring_mode == 1) {
+            a.stage[(long long)shot * a.ringsz + m.w] = out;
+            atomicMax(a.amax + (long long)shot * a.slots + a.slot, __float_as_uint(fabsf(out)));
+        } else {
+            const long long sl = (long long)shot * a.slots + a.slot;
+            a.s2[so + c] = ring_dequant(a.ring16[sl * a.ringsz + m.w], a.scale[sl], a.ring_prec);
+        }
     }
 }
 
-// Ring of one level (used for slot 1 at start-up): ring[ri] = u[cell].
+// Ring of one level (slot 1 at start-up): ring[ri] = u[cell].  With a 16-bit
+// store the values go to the FP32 stage and the slot's max-abs, and the next
+// pad launch quantises them.
 __global__ void k_ring_fill(const float *__restrict__ u, float *__restrict__ ring, long long ss,
-                            long long ring_ss, int NZ, int NX, int P, int N2, int M)
+                            long long ring_ss, int NZ, int NX, int P, int N2, int M,
+                            unsigned *amax, long long amax_ss)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
     if (t >= abc_count(NZ, NX, N2)) return;
     const AbcCell cc = abc_cell(t, NZ, NX, N2);
     const long ri = ring_index(cc.z, cc.x, NZ, NX, N2, M, NZ - 2 * N2, NX - 2 * N2);
-    if (ri >= 0) ring[(long long)shot * ring_ss + ri] = u[(long long)shot * ss + (long)cc.z * P + cc.x];
+    if (ri < 0) return;
+    const float val = u[(long long)shot * ss + (long)cc.z * P + cc.x];
+    ring[(long long)shot * ring_ss + ri] = val;
+    if (amax) atomicMax(amax + (long long)shot * amax_ss, __float_as_uint(fabsf(val)));
 }
 
 // Start of a shot: u0 = 0, u1 = spike at the source (kernel.cu:798-803).
