@@ -129,53 +129,40 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
     }
 }
 
-// Stream one field down the warp's RW rows at the lane's column.  For each
-// row z < NZ the cell gets u2 = 2u1 - u0 + v^2 tao^2/h^2 * L(u1) and `emit`
-// is called with the result.  q is the register queue of the column's rows
-// z-M .. z+M; x-neighbours come from the staged halo box, u0 and v from the
-// staged flat tiles (row i at fr + i*TX).
-template <int MMAX, bool ADAPT, class Emit>
-__device__ __forceinline__ void stream_field(const float *box, const float *f0, const float *fv,
-                                             const StepArgs &a, int zw, int rbase, int cx, int fr,
-                                             Emit emit)
+// Coefficients of one cell: the velocity bin (adaptive) picks a column of the
+// coefficient-major table; with fixed coefficients the table has one column
+// and the values are loaded once per warp into registers (cc).
+template <int MMAX, bool ADAPT>
+__device__ __forceinline__ const float *coef_base(const StepArgs &a, float vc)
 {
-    using S = Shape<MMAX>;
-    constexpr int QN = 2 * MMAX + 1;
-    float q[QN];
-#pragma unroll
-    for (int j = 0; j < QN - 1; ++j) q[j] = box[(rbase + j) * S::BW + cx];
-#pragma unroll
-    for (int i = 0; i < RW; ++i) {
-        q[QN - 1] = box[(rbase + i + QN - 1) * S::BW + cx];
-        const int z = zw + i;
-        if (z < a.NZ) {
-            const float *rowp = box + (rbase + i + MMAX) * S::BW + cx;
-            const float vc = fv[fr + i * TX];
-            const float u0 = f0[fr + i * TX];
-            int bin = 0;
-            if (ADAPT) {
-                bin = (int)((vc - a.vmin) / a.dv + 0.5f);
-                bin = min(max(bin, 0), a.nbins - 1);
-            }
-            const float *cb = a.ctab + bin;
-            const float u = q[MMAX];
-            float w1 = a.k0 * __ldg(cb) * u;
-#pragma unroll
-            for (int l = 1; l <= MMAX; ++l) {
-                const float xs = (q[MMAX - l] + q[MMAX + l]) * a.hzx2_1 + rowp[-l];
-                w1 = fmaf(__ldg(cb + l * a.nbins), xs + rowp[l], w1);
-            }
-            const float vv = vc * vc * a.tao2 * a.h2;
-            emit(i, z, fmaf(vv, w1, 2.0f * u - u0));
-        }
-#pragma unroll
-        for (int j = 0; j < QN - 1; ++j) q[j] = q[j + 1];
+    int bin = 0;
+    if (ADAPT) {
+        bin = (int)((vc - a.vmin) / a.dv + 0.5f);
+        bin = min(max(bin, 0), a.nbins - 1);
     }
+    return a.ctab + bin;
+}
+
+// Spatial operator of one cell: w = k0*c0*u + sum_l c_l*((u[z-l]+u[z+l])*hzx2_1
+// + u[x-l] + u[x+l]) (kernel.cu:59-72), with q the column's register queue
+// (centre at index C) and row the cell's row in the staged halo box.
+template <int MMAX, bool ADAPT>
+__device__ __forceinline__ float lap_cell(const float *q, int C, const float *row, const float *cb,
+                                          const float *cc, int nbins, float k0, float hzx2_1)
+{
+    float w1 = k0 * (ADAPT ? __ldg(cb) : cc[0]) * q[C];
+#pragma unroll
+    for (int l = 1; l <= MMAX; ++l) {
+        const float xs = (q[C - l] + q[C + l]) * hzx2_1 + row[-l];
+        w1 = fmaf(ADAPT ? __ldg(cb + l * nbins) : cc[l], xs + row[l], w1);
+    }
+    return w1;
 }
 
 // One time step of a batch of shots on one 128 x 16 tile (grid: tiles x
 // tiles x shots).  All inputs arrive by TMA into shared memory under one
-// mbarrier; outputs are stored directly.
+// mbarrier; the warp's lanes each own one column and stream its rows through
+// register queues; outputs are stored directly.
 template <int MMAX, bool ADAPT, int MODE>
 __global__ void __launch_bounds__(NTHREADS)
     k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
@@ -185,6 +172,7 @@ __global__ void __launch_bounds__(NTHREADS)
 {
     using S = Shape<MMAX>;
     using SM = Smem<MMAX, MODE>;
+    constexpr int QN = 2 * MMAX + 1;
     extern __shared__ __align__(128) float smem[];
     float *tA = smem;
     float *tS = smem + S::ELEMS;                          // backward only
@@ -216,6 +204,11 @@ __global__ void __launch_bounds__(NTHREADS)
             tma_load_3d(fRa, &img.racc, x0, z0, shot, &bar);
         }
     }
+    // fixed coefficients: once per thread, while the copies are in flight
+    float cc[MMAX + 1];
+#pragma unroll
+    for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
+    const int src = a.src[shot];
     if (!mbar_wait_bounded(&bar, 0, &g_rtm_dev_error)) {
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
         return;
@@ -230,45 +223,83 @@ __global__ void __launch_bounds__(NTHREADS)
     const int cx = S::XH + wx * 32 + lane;   // its column in the halo box
     const int rbase = wz * RW;               // box row of zw - MMAX
     const int fr = wz * RW * TX + wx * 32 + lane;  // flat-tile index of row zw
-    const int src = a.src[shot];
     const int src_z = src / a.NX, src_x = src % a.NX;
     const int N2 = a.N2, NZ = a.NZ, NX = a.NX;
     const bool col_in = gx >= N2 && gx < NX - N2;
     const bool col_ok = gx < NX;
-    const long goff0 = (long)zw * a.P + gx;  // global index of row zw
+    const long long g0 = so + (long)zw * a.P + gx;  // global index of row zw
 
-    // Source field (backward only): interior cells.
-    float sres[RW];
-    if (MODE == MODE_BWD) {
+    if (MODE == MODE_FWD) {
+        // two rows per iteration: two independent accumulation chains
+        float q[QN + 1];
 #pragma unroll
-        for (int i = 0; i < RW; ++i) sres[i] = 0.0f;
-        const bool rows_in = (zw + RW > N2) && (zw < NZ - N2);
-        const bool cols_in = (x0 + wx * 32 + 32 > N2) && (x0 + wx * 32 < NX - N2);
-        if (rows_in && cols_in) {
-            stream_field<MMAX, ADAPT>(tS, fS0, fV, a, zw, rbase, cx, fr,
-                                      [&](int i, int z, float r) {
-                                          if (z < N2 || z >= NZ - N2 || !col_in) return;
-                                          if (z == src_z && gx == src_x) r += a.wavelet;
-                                          a.s2[so + goff0 + (long)i * a.P] = r;
-                                          sres[i] = r;
-                                      });
+        for (int j = 0; j < QN - 1; ++j) q[j] = tA[(rbase + j) * S::BW + cx];
+#pragma unroll
+        for (int i = 0; i < RW; i += 2) {
+            q[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
+            q[QN] = tA[(rbase + i + QN) * S::BW + cx];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int z = zw + i + h;
+                if (z >= NZ) continue;
+                const int t = fr + (i + h) * TX;
+                const float vc = fV[t];
+                const float *cb = coef_base<MMAX, ADAPT>(a, vc);
+                const float *row = tA + (rbase + i + h + MMAX) * S::BW + cx;
+                const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cb, cc, a.nbins, a.k0, a.hzx2_1);
+                float val = fmaf(vc * vc * a.tao2 * a.h2, w1, 2.0f * q[MMAX + h] - fA0[t]);
+                if (z == src_z && gx == src_x) val += a.wavelet;
+                if (col_ok) {
+                    const bool interior = col_in && z >= N2 && z < NZ - N2;
+                    (interior ? a.a2 : a.pre)[g0 + (long)(i + h) * a.P] = val;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < QN - 1; ++j) q[j] = q[j + 2];
         }
+        return;
     }
 
-    // Receiver line within this warp's strip?
+    // Backward: receiver field R on every cell, reconstructed source field S
+    // on the interior, advanced in lockstep so both share the coefficients and
+    // the imaging condition sees both at once.
     bool line_hit = false;
-    if (MODE == MODE_BWD && a.nrec > 0) {
+    if (a.nrec > 0) {
         const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = a.rx0 + (a.nrec - 1) * a.rdx;
         const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(a.rx0, xb), xhi = max(a.rx0, xb);
         line_hit = !(zhi < zw || zlo >= zw + RW || xhi < x0 + wx * 32 || xlo >= x0 + wx * 32 + 32);
     }
-
-    // Field A: u (forward) or R (backward, full grid).
-    stream_field<MMAX, ADAPT>(
-        tA, fA0, fV, a, zw, rbase, cx, fr, [&](int i, int z, float val) {
-            if (!col_ok) return;
-            if (MODE == MODE_FWD && z == src_z && gx == src_x) val += a.wavelet;
-            if (MODE == MODE_BWD && line_hit) {
+    const bool rows_s = (zw + RW > N2) && (zw < NZ - N2);
+    float qr[QN], qs[QN];
+#pragma unroll
+    for (int j = 0; j < QN - 1; ++j) {
+        qr[j] = tA[(rbase + j) * S::BW + cx];
+        qs[j] = rows_s ? tS[(rbase + j) * S::BW + cx] : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < RW; ++i) {
+        qr[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
+        if (rows_s) qs[QN - 1] = tS[(rbase + i + QN - 1) * S::BW + cx];
+        const int z = zw + i;
+        if (z < NZ) {
+            const int t = fr + i * TX;
+            const float vc = fV[t];
+            const float vv = vc * vc * a.tao2 * a.h2;
+            const float *cb = coef_base<MMAX, ADAPT>(a, vc);
+            const float *rowR = tA + (rbase + i + MMAX) * S::BW + cx;
+            const float *rowS = tS + (rbase + i + MMAX) * S::BW + cx;
+            const float c0 = ADAPT ? __ldg(cb) : cc[0];
+            float wr = a.k0 * c0 * qr[MMAX];
+            float ws = a.k0 * c0 * qs[MMAX];
+#pragma unroll
+            for (int l = 1; l <= MMAX; ++l) {
+                const float cl = ADAPT ? __ldg(cb + l * a.nbins) : cc[l];
+                wr = fmaf(cl, (qr[MMAX - l] + qr[MMAX + l]) * a.hzx2_1 + rowR[-l] + rowR[l], wr);
+                if (rows_s)
+                    ws = fmaf(cl, (qs[MMAX - l] + qs[MMAX + l]) * a.hzx2_1 + rowS[-l] + rowS[l], ws);
+            }
+            float rv = fmaf(vv, wr, 2.0f * qr[MMAX] - fA0[t]);
+            if (line_hit) {
                 int j = -1;
                 if (a.rdz == 0) {
                     if (z == a.rz0 && (gx - a.rx0) % a.rdx == 0) j = (gx - a.rx0) / a.rdx;
@@ -280,28 +311,35 @@ __global__ void __launch_bounds__(NTHREADS)
                 }
                 if (j >= 0 && j < a.nrec) {
                     const float d = a.dinj[(long long)shot * a.dstride + j];
-                    if (d != 0.0f) val = d;
+                    if (d != 0.0f) rv = d;
                 }
             }
             const bool interior = col_in && z >= N2 && z < NZ - N2;
-            const long long g = so + goff0 + (long)i * a.P;
-            (interior ? a.a2 : a.pre)[g] = val;
-            if (MODE == MODE_BWD && interior) {
+            const long long g = g0 + (long)i * a.P;
+            if (col_ok) (interior ? a.a2 : a.pre)[g] = rv;
+            if (interior) {
+                float sv = fmaf(vv, ws, 2.0f * qs[MMAX] - fS0[t]);
+                if (z == src_z && gx == src_x) sv += a.wavelet;
+                a.s2[g] = sv;
                 // imaging (kernel.cu:489-517)
-                const int t = fr + i * TX;
-                const float sv = sres[i];
                 if (a.compen) {
                     const float sa = fSa[t] + sv;
-                    const float ra = fRa[t] + val;
+                    const float ra = fRa[t] + rv;
                     a.sacc[g] = sa;
                     a.racc[g] = ra;
                     a.rel1[g] = fR1[t] + ra * sa;
                 } else {
-                    a.rel1[g] = fR1[t] + val * sv;
+                    a.rel1[g] = fR1[t] + rv * sv;
                 }
                 a.rel2[g] = fR2[t] + sv * sv;
             }
-        });
+        }
+#pragma unroll
+        for (int j = 0; j < QN - 1; ++j) {
+            qr[j] = qr[j + 1];
+            qs[j] = qs[j + 1];
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------

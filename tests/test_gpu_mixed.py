@@ -1,7 +1,9 @@
 """Mixed-precision boundary rings (BF16 / FP16 with per-step max-abs
-scaling; stencil and imaging stay FP32) against the FP64 oracle, and the
-FP32 ring path against both oracles.  Errors are relative L2 on the interior
-image (rel1) and illumination (rel2) after one migration."""
+scaling; stencil and imaging stay FP32) against the FP64 oracle.  Errors are
+relative L2 on the interior image (rel1) and illumination (rel2) after one
+migration.  Target: NRMSE <= 1e-3 against FP64 (the FP32 arithmetic alone
+accounts for ~3e-4 here); FP16 rings meet it, BF16 rings (8-bit mantissa)
+land near 2e-3 and are held to 5e-3."""
 import numpy as np
 import pytest
 
@@ -22,8 +24,8 @@ def case():
     return p, seis, d1, d2
 
 
-@pytest.mark.parametrize("prec,tol", [(capi.RTM_RING_F32, 1e-4), (capi.RTM_RING_F16, 1e-3),
-                                      (capi.RTM_RING_BF16, 1e-2)])
+@pytest.mark.parametrize("prec,tol", [(capi.RTM_RING_F32, 1e-3), (capi.RTM_RING_F16, 1e-3),
+                                      (capi.RTM_RING_BF16, 5e-3)])
 def test_ring_precision_vs_fp64(product_lib, cuda_ok, case, prec, tol):
     p, seis, d1, d2 = case
     with Engine(p, batch=2, ring_precision=prec) as e:
