@@ -227,6 +227,19 @@ int rtm_migrate_stack(rtm_ctx *ctx, int nshot, const int *src_cells, const float
                       float whitecoe, int nrec_div, int inorm, float *image, float *illum,
                       float *ups, float *downs, int flags);
 
+/* Uneven aperture windows (reverse-VSP and other geometries where each shot
+ * sees its own part of the survey): the context's model is the whole survey
+ * (nz x nx interior); shot i migrates on interior columns
+ * [win_x0[i], win_x0[i]+win_nx[i]) padded by edge extension as the reference
+ * pads a model it reads (GPU_velocity_real.cpp:20-80).  src_cells[i] is the
+ * flat index z*NX_i + x in the shot's own padded grid (NX_i = win_nx[i]+2*N2);
+ * the context's receiver line moves with the window (columns rx0 - win_x0[i])
+ * and must lie inside it.  Shots of a batch advance together; images are
+ * finished per shot and stacked (Kahan) into the survey frame [nz][nx]. */
+int rtm_migrate_stack_windows(rtm_ctx *ctx, int nshot, const int *src_cells, const int *win_x0,
+                              const int *win_nx, const float *seis, float whitecoe, int nrec_div,
+                              int inorm, float *image, float *illum, int flags);
+
 /* Per-launch timing: with timing enabled, launches go one by one (no graph)
  * with CUDA events around each kernel; rtm_ctx_timing returns the summed
  * milliseconds and launch counts of [0] forward stencil, [1] backward

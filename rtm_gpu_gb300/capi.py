@@ -91,6 +91,7 @@ def lib():
         L.rtm_model_batch.argtypes = [vp, I, ip, vp, I]
         L.rtm_migrate_batch.argtypes = [vp, I, ip, vp, vp, vp, I]
         L.rtm_migrate_stack.argtypes = [vp, I, ip, vp, F, I, I, vp, vp, vp, vp, I]
+        L.rtm_migrate_stack_windows.argtypes = [vp, I, ip, ip, ip, vp, F, I, I, vp, vp, I]
         L.rtm_ctx_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_long)]
         L.rtm_ctx_set_timing.argtypes = [vp, I]
         L.rtm_ctx_launches.argtypes = [vp, C.POINTER(C.c_long), I]

@@ -88,7 +88,16 @@ struct rtm_ctx {
     float *img = nullptr, *ill = nullptr;
     CUtensorMap mapS[3], mapR[3];      // halo boxes of the rotating levels
     CUtensorMap flatS[3], flatR[3];    // flat tiles of the same buffers
-    CUtensorMap flatV;                 // flat tiles of the model
+    CUtensorMap flatV;                 // flat tiles of the model (shared by the batch)
+    CUtensorMap flatVs;                // flat tiles of the per-shot window models
+    // per-shot geometry of the current batch (device): padded width, window
+    // start column in the survey interior, receiver start column
+    int *gnx = nullptr, *gxa = nullptr, *grx0 = nullptr;
+    std::vector<int> hnx, hxa;         // host copies for the current batch
+    bool windowed = false;             // current batch uses per-shot models
+    float *vs = nullptr, *r1s = nullptr;          // [B][NZ][P] window models
+    int4 *meta_s = nullptr;
+    float4 *fac_s = nullptr;                      // [B][nabc] window pad tables
     eng::ImgMaps imaps;                // flat tiles of the imaging accumulators
     size_t bytes = 0;
     // graphs keyed by (phase, batch)
@@ -129,6 +138,12 @@ void free_all(rtm_ctx *c)
     for (float *p : fl)
         if (p) cudaFree(p);
     if (c->src) cudaFree(c->src);
+    for (int *q : {c->gnx, c->gxa, c->grx0})
+        if (q) cudaFree(q);
+    if (c->vs) cudaFree(c->vs);
+    if (c->r1s) cudaFree(c->r1s);
+    if (c->meta_s) cudaFree(c->meta_s);
+    if (c->fac_s) cudaFree(c->fac_s);
     if (c->ring16) cudaFree(c->ring16);
     if (c->rstage) cudaFree(c->rstage);
     if (c->rscale) cudaFree(c->rscale);
@@ -157,7 +172,7 @@ int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb)
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
     eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(*m.A, *m.S, *m.A0, *m.S0,
-                                                                      c->flatV, c->imaps, a);
+                                                                      c->windowed ? c->flatVs : c->flatV, c->imaps, a);
     return RTM_OK;
 }
 
@@ -219,15 +234,19 @@ eng::StepArgs base_step(rtm_ctx *c)
     a.v = c->v; a.ctab = c->ctab; a.src = c->src; a.compen = c->p.compen;
     a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = 0;
     a.rel1 = c->rel1; a.rel2 = c->rel2; a.sacc = c->sacc; a.racc = c->racc;
+    a.nxs = c->gnx; a.rx0s = c->grx0; a.vshot = c->windowed ? 1 : 0;
     return a;
 }
 
 eng::PadArgs base_pad(rtm_ctx *c)
 {
     eng::PadArgs a{};
-    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2;
+    a.NZ = c->NZ; a.P = c->P; a.N2 = c->N2;
     a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
-    a.meta = c->pad_meta; a.fac = c->pad_fac;
+    a.nxs = c->gnx; a.rx0s = c->grx0;
+    a.meta = c->windowed ? c->meta_s : c->pad_meta;
+    a.fac = c->windowed ? c->fac_s : c->pad_fac;
+    a.tab_ss = c->windowed ? a.nabc : 0;
     a.pre = c->pre;
     a.ring_prec = c->p.ring_precision;
     a.ringsz = c->ringsz;
@@ -266,7 +285,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     const long long ss = c->ss;
     const int NT = c->NT;
     eng::k_shot_init<<<dim3(cdiv(ss, 256), nb), 256, 0, c->st>>>(c->S[0], c->S[1], c->S[2], c->pre,
-                                                                 c->src, c->p.spike, ss, c->NX, c->P);
+                                                                 c->src, c->gnx, c->p.spike, ss, c->P);
     c->launches++;
     const bool r16 = c->p.ring_precision != RTM_RING_F32;
     const long long bstage = (long long)c->B * c->ringsz;  // floats of one stage parity
@@ -275,18 +294,18 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     if (c->M > 0) {
         if (r16)
             eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
-                c->S[1], c->rstage + 1 * bstage, ss, c->ringsz, c->NZ, c->NX, c->P, c->N2, c->M,
+                c->S[1], c->rstage + 1 * bstage, ss, c->ringsz, c->NZ, c->gnx, c->P, c->N2, c->M,
                 c->ramax + 1, NT);
         else
             eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
-                c->S[1], c->ring + c->ringsz, ss, (long long)NT * c->ringsz, c->NZ, c->NX, c->P, c->N2,
+                c->S[1], c->ring + c->ringsz, ss, (long long)NT * c->ringsz, c->NZ, c->gnx, c->P, c->N2,
                 c->M, nullptr, 0);
     }
     c->launches += (c->M > 0);
     const long long rss = (long long)NT * c->nrec;
     if (rec_on && c->nrec > 0) {
         eng::k_record<<<dim3(cdiv(c->nrec, 128), nb), 128, 0, c->st>>>(
-            c->S[0], c->rec, ss, rss, c->P, c->p.rz0, c->p.rx0, c->p.rdz, c->p.rdx, c->nrec);
+            c->S[0], c->rec, ss, rss, c->P, c->p.rz0, c->grx0, c->p.rdz, c->p.rdx, c->nrec);
         c->launches++;
     }
     RTM_LAUNCH_CHECK();
@@ -320,7 +339,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     if (rec_on && c->nrec > 0)
         eng::k_record<<<dim3(cdiv(c->nrec, 128), nb), 128, 0, c->st>>>(
             c->S[(NT - 1) % 3], c->rec + (long long)(NT - 1) * c->nrec, ss, rss, c->P, c->p.rz0,
-            c->p.rx0, c->p.rdz, c->p.rdx, c->nrec);
+            c->grx0, c->p.rdz, c->p.rdx, c->nrec);
     c->launches += (rec_on && c->nrec > 0);
     RTM_LAUNCH_CHECK();
     return RTM_OK;
@@ -334,8 +353,8 @@ int enqueue_backward(rtm_ctx *c, int nb)
     const int NT = c->NT;
     float *F1 = c->S[(NT - 1) % 3], *F0 = c->S[(NT - 2) % 3];
     eng::k_img_init<<<dim3(cdiv(ss, 256), nb), 256, 0, c->st>>>(
-        F1, F0, c->R[0], c->R[1], c->R[2], c->rel1, c->rel2, c->sacc, c->racc, c->src, c->p.spike,
-        c->p.compen, ss, c->NX, c->P);
+        F1, F0, c->R[0], c->R[1], c->R[2], c->rel1, c->rel2, c->sacc, c->racc, c->src, c->gnx,
+        c->p.spike, c->p.compen, ss, c->P);
     c->launches++;
     RTM_LAUNCH_CHECK();
     eng::StepArgs sa = base_step(c);
@@ -378,7 +397,7 @@ int run_phase(rtm_ctx *c, int phase, int nb, int flags)
         return enqueue_backward(c, nb);
     };
     if (!use_graph) return body();
-    auto key = std::make_pair(phase, nb);
+    auto key = std::make_pair(phase * 2 + (c->windowed ? 1 : 0), nb);
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
         cudaGraph_t g;
@@ -404,16 +423,66 @@ int run_phase(rtm_ctx *c, int phase, int nb, int flags)
     return RTM_OK;
 }
 
-int upload_src(rtm_ctx *c, int nb, const int *src_cells)
+// Sets the per-shot geometry of the next batch: window start column xa and
+// interior width nx of each shot (NULL: the whole survey grid), sources in
+// each shot's own padded grid.  Windowed batches get their models and pad
+// tables built on the device.
+int set_batch(rtm_ctx *c, int nb, const int *src_cells, const int *xa, const int *nx)
 {
+    c->hnx.assign(nb, c->NX);
+    c->hxa.assign(nb, 0);
+    std::vector<int> rx0(nb, c->p.rx0);
+    bool windowed = false;
     for (int i = 0; i < nb; ++i) {
-        const int s = src_cells[i];
-        if (s < 0 || s >= c->NZ * c->NX) {
-            rtm_set_last_error("source cell outside the grid");
+        if (xa && nx) {
+            if (nx[i] < 2 * c->MM + 2 || xa[i] < 0 || xa[i] + nx[i] > c->nx) {
+                rtm_set_last_error("aperture window outside the survey");
+                return RTM_ERR_ARG;
+            }
+            c->hxa[i] = xa[i];
+            c->hnx[i] = nx[i] + 2 * c->N2;
+            rx0[i] = c->p.rx0 - xa[i];
+            windowed = windowed || xa[i] != 0 || nx[i] != c->nx;
+        }
+        const int NXi = c->hnx[i];
+        if (src_cells[i] < 0 || src_cells[i] >= c->NZ * NXi) {
+            rtm_set_last_error("source cell outside the shot's grid");
             return RTM_ERR_ARG;
         }
+        for (int j = 0; j < c->nrec; j += std::max(1, c->nrec - 1)) {
+            const int x = rx0[i] + j * c->p.rdx;
+            if (x < 0 || x >= NXi) {
+                rtm_set_last_error("receivers outside the shot's aperture window");
+                return RTM_ERR_ARG;
+            }
+        }
     }
+    std::vector<int> hn(c->hnx);
     RTM_CUDA_TRY(cudaMemcpyAsync(c->src, src_cells, sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
+    RTM_CUDA_TRY(cudaMemcpyAsync(c->gnx, hn.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
+    RTM_CUDA_TRY(cudaMemcpyAsync(c->gxa, c->hxa.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
+    RTM_CUDA_TRY(cudaMemcpyAsync(c->grx0, rx0.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
+    // the host vectors must outlive the async copies
+    RTM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->windowed = windowed;
+    if (!windowed) return RTM_OK;
+    if (!c->vs) {
+        const size_t bgrid = (size_t)c->ss * c->B;
+        const long nabc = abc_count(c->NZ, c->NX, c->N2);
+        if (int rc = dalloc(c, &c->vs, bgrid)) return rc;
+        if (int rc = dalloc(c, &c->r1s, bgrid)) return rc;
+        if (int rc = dalloc(c, &c->meta_s, (size_t)nabc * c->B)) return rc;
+        if (int rc = dalloc(c, &c->fac_s, (size_t)nabc * c->B)) return rc;
+        if (int rc = make_map(&c->flatVs, c->vs, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ)) return rc;
+    }
+    const long nabc = abc_count(c->NZ, c->NX, c->N2);
+    eng::k_window_model<<<dim3(cdiv(c->ss, 256), nb), 256, 0, c->st>>>(
+        c->v, c->r1, c->P, c->gxa, c->gnx, c->vs, c->r1s, c->ss, c->NZ, c->P, c->N2);
+    eng::k_pad_tables<<<dim3(cdiv(nabc, 256), nb), 256, 0, c->st>>>(
+        c->vs, c->r1s, c->w, c->gnx, c->ss, nabc, c->NZ, c->P, c->N2, c->M, c->p.taoh, c->p.taoh2,
+        c->p.quirk, c->meta_s, c->fac_s);
+    c->launches += 2;
+    RTM_LAUNCH_CHECK();
     return RTM_OK;
 }
 
@@ -570,6 +639,9 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     TRY(dalloc(c, &c->rec, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
     TRY(dalloc(c, &c->stage, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
     TRY(dalloc(c, &c->src, (size_t)c->B));
+    TRY(dalloc(c, &c->gnx, (size_t)c->B));
+    TRY(dalloc(c, &c->gxa, (size_t)c->B));
+    TRY(dalloc(c, &c->grx0, (size_t)c->B));
     TRY(dalloc(c, &c->imax, (size_t)c->B));
     TRY(dalloc(c, &c->ups, (size_t)c->B * c->nz * c->nx));
     TRY(dalloc(c, &c->downs, (size_t)c->B * c->nz * c->nx));
@@ -715,7 +787,7 @@ int rtm_model_batch(rtm_ctx *c, int nshot, const int *src_cells, float *rec, int
     const long long per = (long long)c->NT * c->nrec;
     for (int s0 = 0; s0 < nshot; s0 += c->B) {
         const int nb = std::min(c->B, nshot - s0);
-        if (int rc = upload_src(c, nb, src_cells + s0)) return rc;
+        if (int rc = set_batch(c, nb, src_cells + s0, nullptr, nullptr)) return rc;
         if (int rc = run_phase(c, 0, nb, flags)) return rc;
         if (c->nrec > 0) {
             transpose(c, c->rec, c->stage, c->NT, c->nrec, nb);
@@ -733,11 +805,13 @@ int rtm_model_batch(rtm_ctx *c, int nshot, const int *src_cells, float *rec, int
     return RTM_OK;
 }
 
-static int migrate_group(rtm_ctx *c, int s0, int nb, const int *src_cells, const float *seis, int flags)
+static int migrate_group(rtm_ctx *c, int s0, int nb, const int *src_cells, const int *xa,
+                         const int *nx, const float *seis, int flags)
 {
     const bool dev = flags & RTM_DEVICE_PTRS;
     const long long per = (long long)c->NT * c->nrec;
-    if (int rc = upload_src(c, nb, src_cells + s0)) return rc;
+    if (int rc = set_batch(c, nb, src_cells + s0, xa ? xa + s0 : nullptr, nx ? nx + s0 : nullptr))
+        return rc;
     if (c->nrec > 0) {
         RTM_CUDA_TRY(cudaMemcpyAsync(c->stage, seis + (long long)s0 * per, sizeof(float) * per * nb,
                                      dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
@@ -754,7 +828,7 @@ int rtm_migrate_batch(rtm_ctx *c, int nshot, const int *src_cells, const float *
     const long long gsz = (long long)c->NZ * c->NX;
     for (int s0 = 0; s0 < nshot; s0 += c->B) {
         const int nb = std::min(c->B, nshot - s0);
-        if (int rc = migrate_group(c, s0, nb, src_cells, seis, flags)) return rc;
+        if (int rc = migrate_group(c, s0, nb, src_cells, nullptr, nullptr, seis, flags)) return rc;
         if (rel1)
             if (int rc = copy_grid_out(c, c->rel1, rel1 + s0 * gsz, nb, dev)) return rc;
         if (rel2)
@@ -770,25 +844,27 @@ int rtm_migrate_batch(rtm_ctx *c, int nshot, const int *src_cells, const float *
     return RTM_OK;
 }
 
-int rtm_migrate_stack(rtm_ctx *c, int nshot, const int *src_cells, const float *seis,
-                      float whitecoe, int nrec_div, int inorm, float *image, float *illum,
-                      float *ups, float *downs, int flags)
+static int migrate_stack_impl(rtm_ctx *c, int nshot, const int *src_cells, const int *xa,
+                              const int *nx, const float *seis, float whitecoe, int nrec_div,
+                              int inorm, float *image, float *illum, float *ups, float *downs,
+                              int flags)
 {
     if (!c || nshot < 1 || !src_cells || (!seis && c->nrec > 0) || nrec_div < 1) return RTM_ERR_ARG;
     const bool dev = flags & RTM_DEVICE_PTRS;
-    const long ncell = (long)c->nz * c->nx;
+    const long ncell = (long)c->nz * c->nx;  // survey interior
     for (float *q : {c->ks1, c->kc1, c->ks2, c->kc2})
         RTM_CUDA_TRY(cudaMemsetAsync(q, 0, sizeof(float) * ncell, c->st));
     for (int s0 = 0; s0 < nshot; s0 += c->B) {
         const int nb = std::min(c->B, nshot - s0);
-        if (int rc = migrate_group(c, s0, nb, src_cells, seis, flags)) return rc;
+        if (int rc = migrate_group(c, s0, nb, src_cells, xa, nx, seis, flags)) return rc;
         RTM_CUDA_TRY(cudaMemsetAsync(c->imax, 0, sizeof(unsigned) * nb, c->st));
-        eng::k_illum_max<<<dim3(64, nb), 256, 0, c->st>>>(c->rel2, c->imax, c->ss, c->NZ, c->NX, c->P,
-                                                          c->N2);
+        eng::k_illum_max<<<dim3(64, nb), 256, 0, c->st>>>(c->rel2, c->imax, c->ss, c->NZ, c->gnx,
+                                                          c->P, c->N2);
         eng::k_finish<<<dim3(cdiv(ncell, 256), nb), 256, 0, c->st>>>(
-            c->rel1, c->rel2, c->v, c->imax, c->ups, c->downs, c->ss, c->NZ, c->NX, c->P, c->N2,
-            c->vmax, whitecoe);
-        eng::k_stack_kahan<<<cdiv(ncell, 256), 256, 0, c->st>>>(c->ups, c->downs, nb, ncell, c->ks1,
+            c->rel1, c->rel2, c->windowed ? c->vs : c->v, c->windowed ? c->ss : 0, c->imax, c->ups,
+            c->downs, c->ss, c->NZ, c->gnx, c->P, c->N2, c->nx, c->vmax, whitecoe);
+        eng::k_stack_kahan<<<cdiv(ncell, 256), 256, 0, c->st>>>(c->ups, c->downs, nb, c->nz, c->nx,
+                                                               c->nx, c->gxa, c->gnx, c->N2, c->ks1,
                                                                c->kc1, c->ks2, c->kc2);
         c->launches += 3;
         RTM_LAUNCH_CHECK();
@@ -815,6 +891,23 @@ int rtm_migrate_stack(rtm_ctx *c, int nshot, const int *src_cells, const float *
         return RTM_ERR_DEVICE;
     }
     return RTM_OK;
+}
+
+int rtm_migrate_stack(rtm_ctx *c, int nshot, const int *src_cells, const float *seis,
+                      float whitecoe, int nrec_div, int inorm, float *image, float *illum,
+                      float *ups, float *downs, int flags)
+{
+    return migrate_stack_impl(c, nshot, src_cells, nullptr, nullptr, seis, whitecoe, nrec_div,
+                              inorm, image, illum, ups, downs, flags);
+}
+
+int rtm_migrate_stack_windows(rtm_ctx *c, int nshot, const int *src_cells, const int *win_x0,
+                              const int *win_nx, const float *seis, float whitecoe, int nrec_div,
+                              int inorm, float *image, float *illum, int flags)
+{
+    if (!win_x0 || !win_nx) return RTM_ERR_ARG;
+    return migrate_stack_impl(c, nshot, src_cells, win_x0, win_nx, seis, whitecoe, nrec_div, inorm,
+                              image, illum, nullptr, nullptr, flags);
 }
 
 }  // extern "C"

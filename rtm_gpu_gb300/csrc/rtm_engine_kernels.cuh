@@ -92,6 +92,10 @@ struct StepArgs {
     int rz0, rx0, rdz, rdx, nrec;
     const float *dinj;         // data row for this step, shot 0; shot s at + s*dstride
     long long dstride;
+    // per-shot geometry: padded width and receiver start column of each
+    // shot's grid; vshot = 1 when every shot has its own model copy
+    const int *nxs, *rx0s;
+    int vshot;
 };
 
 __device__ __forceinline__ int mirror_i(int i, int n)
@@ -184,6 +188,8 @@ __global__ void __launch_bounds__(NTHREADS)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wx = warp % WX, wz = warp / WX;
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z;
+    const int NX = a.nxs[shot];
+    if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
 
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -194,7 +200,7 @@ __global__ void __launch_bounds__(NTHREADS)
         mbar_arrive_expect_tx(&bar, SM::BYTES - 16u);
         tma_load_3d(tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, &bar);
         tma_load_3d(fA0, &flatA0, x0, z0, shot, &bar);
-        tma_load_3d(fV, &flatV, x0, z0, 0, &bar);
+        tma_load_3d(fV, &flatV, x0, z0, a.vshot ? shot : 0, &bar);
         if (MODE == MODE_BWD) {
             tma_load_3d(tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, &bar);
             tma_load_3d(fS0, &flatS0, x0, z0, shot, &bar);
@@ -213,8 +219,8 @@ __global__ void __launch_bounds__(NTHREADS)
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
         return;
     }
-    patch_halo<MMAX>(tA, x0, z0, a.NX, a.NZ);
-    if (MODE == MODE_BWD) patch_halo<MMAX>(tS, x0, z0, a.NX, a.NZ);
+    patch_halo<MMAX>(tA, x0, z0, NX, a.NZ);
+    if (MODE == MODE_BWD) patch_halo<MMAX>(tS, x0, z0, NX, a.NZ);
     __syncthreads();
 
     const long long so = (long long)shot * a.ss;
@@ -223,8 +229,9 @@ __global__ void __launch_bounds__(NTHREADS)
     const int cx = S::XH + wx * 32 + lane;   // its column in the halo box
     const int rbase = wz * RW;               // box row of zw - MMAX
     const int fr = wz * RW * TX + wx * 32 + lane;  // flat-tile index of row zw
-    const int src_z = src / a.NX, src_x = src % a.NX;
-    const int N2 = a.N2, NZ = a.NZ, NX = a.NX;
+    const int src_z = src / NX, src_x = src % NX;
+    const int N2 = a.N2, NZ = a.NZ;
+    const int rx0 = a.rx0s[shot];
     const bool col_in = gx >= N2 && gx < NX - N2;
     const bool col_ok = gx < NX;
     const long long g0 = so + (long)zw * a.P + gx;  // global index of row zw
@@ -265,8 +272,8 @@ __global__ void __launch_bounds__(NTHREADS)
     // the imaging condition sees both at once.
     bool line_hit = false;
     if (a.nrec > 0) {
-        const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = a.rx0 + (a.nrec - 1) * a.rdx;
-        const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(a.rx0, xb), xhi = max(a.rx0, xb);
+        const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = rx0 + (a.nrec - 1) * a.rdx;
+        const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(rx0, xb), xhi = max(rx0, xb);
         line_hit = !(zhi < zw || zlo >= zw + RW || xhi < x0 + wx * 32 || xlo >= x0 + wx * 32 + 32);
     }
     const bool rows_s = (zw + RW > N2) && (zw < NZ - N2);
@@ -302,11 +309,11 @@ __global__ void __launch_bounds__(NTHREADS)
             if (line_hit) {
                 int j = -1;
                 if (a.rdz == 0) {
-                    if (z == a.rz0 && (gx - a.rx0) % a.rdx == 0) j = (gx - a.rx0) / a.rdx;
+                    if (z == a.rz0 && (gx - rx0) % a.rdx == 0) j = (gx - rx0) / a.rdx;
                 } else if (a.rdx == 0) {
-                    if (gx == a.rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
-                } else if ((gx - a.rx0) % a.rdx == 0) {
-                    const int jj = (gx - a.rx0) / a.rdx;
+                    if (gx == rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
+                } else if ((gx - rx0) % a.rdx == 0) {
+                    const int jj = (gx - rx0) / a.rdx;
                     if (z == a.rz0 + jj * a.rdz) j = jj;
                 }
                 if (j >= 0 && j < a.nrec) {
@@ -347,9 +354,11 @@ __global__ void __launch_bounds__(NTHREADS)
 // ring save / restore, receiver recording.
 
 struct PadArgs {
-    int NZ, NX, P, N2;
+    int NZ, P, N2;
     long long ss;
-    long nabc;
+    long nabc;                // pad cells of the widest grid (threads per shot)
+    const int *nxs, *rx0s;    // per-shot padded width and receiver start column
+    long long tab_ss;         // pad-table entries between shots (0: shared table)
     const int4 *meta;         // [nabc] {z, x, kind | dz<<2 | dx<<4, ring slot index or -1}
     const float4 *fac;        // [nabc] side: {taoh*v, 1/(taoh*v+1), taoh2*vq*vq, w}
                               //        corner: {r_1, 1/(2 r_1+1), 0, w}
@@ -425,10 +434,11 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
     const long long so = (long long)shot * a.ss;
+    const int NX = a.nxs[shot];
     if (t >= a.nabc) {
         long j = t - a.nabc;
         if (a.rec && j < a.nrec) {
-            const int z = a.rz0 + (int)j * a.rdz, x = a.rx0 + (int)j * a.rdx;
+            const int z = a.rz0 + (int)j * a.rdz, x = a.rx0s[shot] + (int)j * a.rdx;
             a.rec[(long long)shot * a.rec_ss + j] = a.a1[so + (long)z * a.P + x];
             return;
         }
@@ -442,11 +452,12 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         }
         return;
     }
-    const int4 m = __ldg(a.meta + t);
-    const float4 f = __ldg(a.fac + t);
+    if (t >= abc_count(a.NZ, NX, a.N2)) return;  // this shot's pad is smaller
+    const int4 m = __ldg(a.meta + shot * a.tab_ss + t);
+    const float4 f = __ldg(a.fac + shot * a.tab_ss + t);
     const int z = m.x, x = m.y, kind = m.z & 3;
     const int dz = ((m.z >> 2) & 3) == 1 ? 1 : -1, dx = ((m.z >> 4) & 3) == 1 ? 1 : -1;
-    const int NZ = a.NZ, NX = a.NX, N2 = a.N2, P = a.P;
+    const int NZ = a.NZ, N2 = a.N2, P = a.P;
     const long c = (long)z * P + x;
     const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so, *in2 = a.a2 + so;
     auto pv = [&](int zz, int xx) -> float {
@@ -492,11 +503,12 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
 // store the values go to the FP32 stage and the slot's max-abs, and the next
 // pad launch quantises them.
 __global__ void k_ring_fill(const float *__restrict__ u, float *__restrict__ ring, long long ss,
-                            long long ring_ss, int NZ, int NX, int P, int N2, int M,
+                            long long ring_ss, int NZ, const int *nxs, int P, int N2, int M,
                             unsigned *amax, long long amax_ss)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
+    const int NX = nxs[shot];
     if (t >= abc_count(NZ, NX, N2)) return;
     const AbcCell cc = abc_cell(t, NZ, NX, N2);
     const long ri = ring_index(cc.z, cc.x, NZ, NX, N2, M, NZ - 2 * N2, NX - 2 * N2);
@@ -508,7 +520,7 @@ __global__ void k_ring_fill(const float *__restrict__ u, float *__restrict__ rin
 
 // Start of a shot: u0 = 0, u1 = spike at the source (kernel.cu:798-803).
 __global__ void k_shot_init(float *u0, float *u1, float *u2, float *pre, const int *src,
-                            float spike, long long ss, int NX, int P)
+                            const int *nxs, float spike, long long ss, int P)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
@@ -517,7 +529,7 @@ __global__ void k_shot_init(float *u0, float *u1, float *u2, float *pre, const i
     u0[o] = 0.0f;
     u2[o] = 0.0f;
     pre[o] = 0.0f;
-    const int s = src[shot];
+    const int s = src[shot], NX = nxs[shot];
     const long si = (long)(s / NX) * P + s % NX;
     u1[o] = (i == si) ? spike : 0.0f;
 }
@@ -528,13 +540,13 @@ __global__ void k_shot_init(float *u0, float *u1, float *u2, float *pre, const i
 // the start spike at the source).
 __global__ void k_img_init(const float *F1, const float *F0, float *R0, float *R1, float *R2,
                            float *rel1, float *rel2, float *sacc, float *racc, const int *src,
-                           float spike, int compen, long long ss, int NX, int P)
+                           const int *nxs, float spike, int compen, long long ss, int P)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
     if (i >= ss) return;
     const long long o = (long long)shot * ss + i;
-    const int s = src[shot];
+    const int s = src[shot], NX = nxs[shot];
     const long si = (long)(s / NX) * P + s % NX;
     const float h1 = (i == si) ? spike : 0.0f, h0 = 0.0f;
     const float b0 = F1[o], b1 = F0[o];  // BW0 = u_{NT-1}, BW1 = u_{NT-2}
@@ -555,22 +567,88 @@ __global__ void k_img_init(const float *F1, const float *F0, float *R0, float *R
 
 // Receiver samples of a level (used for the first and last recorded steps).
 __global__ void k_record(const float *u, float *rec, long long ss, long long rec_ss, int P, int rz0,
-                         int rx0, int rdz, int rdx, int nrec)
+                         const int *rx0s, int rdz, int rdx, int nrec)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
     if (j >= nrec) return;
-    const int z = rz0 + j * rdz, x = rx0 + j * rdx;
+    const int z = rz0 + j * rdz, x = rx0s[shot] + j * rdx;
     rec[(long long)shot * rec_ss + j] = u[(long long)shot * ss + (long)z * P + x];
+}
+
+// Model of each shot's aperture window: interior columns [xa, xa+nx) of the
+// survey model, padded by edge extension as the reference pads a model it
+// reads (GPU_velocity_real.cpp:20-80); v and r_1 copied from the survey's
+// padded grid (survey pitch Pg) so the values are bit-identical.
+__global__ void k_window_model(const float *vg, const float *r1g, int Pg, const int *xas,
+                               const int *nxs, float *vs, float *r1s, long long ss, int NZ, int P,
+                               int N2)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    if (i >= ss) return;
+    const int z = (int)(i / P), x = (int)(i % P);
+    const int NX = nxs[shot], nx = NX - 2 * N2;
+    const int xi = min(max(x - N2, 0), nx - 1);   // pitch columns repeat the last column
+    const long gi = (long)z * Pg + N2 + xas[shot] + xi;
+    const long long o = (long long)shot * ss + i;
+    const int zc = min(max(z, N2), NZ - N2 - 1);
+    const long gz = (long)zc * Pg + N2 + xas[shot] + xi;
+    vs[o] = vg[(z >= N2 && z < NZ - N2) ? gi : gz];
+    r1s[o] = r1g[(z >= N2 && z < NZ - N2) ? gi : gz];
+}
+
+// Pad tables of each shot's grid (the device form of the table rtm_ctx_create
+// builds for a single grid): classification, inward directions, ring slot and
+// the model factors, from the shot's own padded model.
+__global__ void k_pad_tables(const float *vs, const float *r1s, const float *w, const int *nxs,
+                             long long ss, long long tab_ss, int NZ, int P, int N2, int M,
+                             float taoh, float taoh2, int quirk, int4 *meta, float4 *fac)
+{
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int shot = blockIdx.y;
+    const int NX = nxs[shot];
+    if (t >= abc_count(NZ, NX, N2)) return;
+    const AbcCell cc = abc_cell(t, NZ, NX, N2);
+    const int z = cc.z, x = cc.x;
+    const int ea = min(z, NZ - 1 - z), ee = min(x, NX - 1 - x);
+    const int dz = (z < NZ - 1 - z) ? 1 : -1, dx = (x < NX - 1 - x) ? 1 : -1;
+    int kind;
+    long q = (long)z * NX + x;  // flat index (reference pitch NX) of the lateral-term velocity
+    if (ee >= ea + 2) {
+        kind = PAD_ROWEDGE;
+        if (quirk && dz < 0) q = (long)(NZ - 1 - z) * NX + x;
+    } else if (ea >= ee + 2) {
+        kind = PAD_COLEDGE;
+        if (quirk) q = (dx > 0) ? (long)x * NX + z : (long)(NX - 1 - x) * NX + z;
+    } else {
+        kind = PAD_CORNER;
+    }
+    const float *v = vs + shot * ss, *r1 = r1s + shot * ss;
+    const float wj = w[blend_index(z, x, NZ, NX, N2)];
+    float4 f;
+    if (kind == PAD_CORNER) {
+        const float rr = r1[(long)z * P + x];
+        f = make_float4(rr, __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(2.0f, rr), 1.0f)), 0.0f, wj);
+    } else {
+        const float vc = v[(long)z * P + x];
+        const float vq = v[(q / NX) * P + q % NX];
+        const float tv = __fmul_rn(taoh, vc);
+        f = make_float4(tv, __fdiv_rn(1.0f, __fadd_rn(tv, 1.0f)), __fmul_rn(__fmul_rn(taoh2, vq), vq), wj);
+    }
+    const long ri = M > 0 ? ring_index(z, x, NZ, NX, N2, M, NZ - 2 * N2, NX - 2 * N2) : -1;
+    meta[shot * tab_ss + t] = make_int4(z, x, kind | ((dz > 0 ? 1 : 2) << 2) | ((dx > 0 ? 1 : 2) << 4), (int)ri);
+    fac[shot * tab_ss + t] = f;
 }
 
 // ---------------------------------------------------------------------------
 // Per-shot finishing (kernel.cu:935-990) and the compensated stack.
 
-__global__ void k_illum_max(const float *rel2, unsigned *mx, long long ss, int NZ, int NX, int P, int N2)
+__global__ void k_illum_max(const float *rel2, unsigned *mx, long long ss, int NZ, const int *nxs,
+                            int P, int N2)
 {
     const int shot = blockIdx.y;
-    const int nz = NZ - 2 * N2, nx = NX - 2 * N2;
+    const int nz = NZ - 2 * N2, nx = nxs[shot] - 2 * N2;
     float m = 0.0f;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < (long)nz * nx;
          t += (long)gridDim.x * blockDim.x) {
@@ -583,14 +661,16 @@ __global__ void k_illum_max(const float *rel2, unsigned *mx, long long ss, int N
 }
 
 // up = -(Laplacian of rel1) * v^2 / vmax^2 with even reflection at the
-// interior edges, down = rel2 + whitecoe*max|rel2|; outputs [shot][nz][nx].
-__global__ void k_finish(const float *rel1, const float *rel2, const float *v, const unsigned *mx,
-                         float *up, float *down, long long ss, int NZ, int NX, int P, int N2,
-                         float vmax, float whitecoe)
+// interior edges, down = rel2 + whitecoe*max|rel2|; outputs
+// [shot][nz][ostride] (ostride >= the shot's interior width).
+__global__ void k_finish(const float *rel1, const float *rel2, const float *v, long long vss,
+                         const unsigned *mx, float *up, float *down, long long ss, int NZ,
+                         const int *nxs, int P, int N2, int ostride, float vmax, float whitecoe)
 {
+    const int shot = blockIdx.y;
+    const int NX = nxs[shot];
     const int nz = NZ - 2 * N2, nx = NX - 2 * N2;
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int shot = blockIdx.y;
     if (t >= (long)nz * nx) return;
     const int zi = (int)(t / nx), xi = (int)(t % nx);
     const int i = zi + N2, j = xi + N2;
@@ -602,27 +682,33 @@ __global__ void k_finish(const float *rel1, const float *rel2, const float *v, c
     const float *g = rel1 + (long long)shot * ss;
     const float s = g[(long)i * P + j2] + g[(long)i * P + j1] + g[(long)i2 * P + j] +
                     g[(long)i1 * P + j] - 4.0f * g[(long)i * P + j];
-    const float vv = v[(long)i * P + j];
-    const long long o = (long long)shot * nz * nx + t;
+    const float vv = v[shot * vss + (long)i * P + j];
+    const long long o = ((long long)shot * nz + zi) * ostride + xi;
     up[o] = -1.0f * s * vv * vv / (vmax * vmax);
     const float stable = __uint_as_float(mx[shot]) * whitecoe;
     down[o] = rel2[(long long)shot * ss + (long)i * P + j] + stable;
 }
 
-// Compensated (Kahan) accumulation of per-shot images in shot order:
+// Compensated (Kahan) accumulation of per-shot images into the survey frame,
+// in shot order; shot m covers survey columns [xa[m], xa[m]+nx_m).
 // sum/comp persist across batches.
-__global__ void k_stack_kahan(const float *up, const float *down, int nshot, long ncell,
-                              float *s1, float *c1, float *s2, float *c2)
+__global__ void k_stack_kahan(const float *up, const float *down, int nshot, int nz, int nxg,
+                              int ostride, const int *xas, const int *nxs, int N2, float *s1,
+                              float *c1, float *s2, float *c2)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ncell) return;
+    if (t >= (long)nz * nxg) return;
+    const int zi = (int)(t / nxg), xg = (int)(t % nxg);
     float a1 = s1[t], e1 = c1[t], a2 = s2[t], e2 = c2[t];
     for (int m = 0; m < nshot; ++m) {
-        const float y1 = __fsub_rn(up[(long)m * ncell + t], e1);
+        const int xi = xg - xas[m];
+        if (xi < 0 || xi >= nxs[m] - 2 * N2) continue;
+        const long long o = ((long long)m * nz + zi) * ostride + xi;
+        const float y1 = __fsub_rn(up[o], e1);
         const float t1 = __fadd_rn(a1, y1);
         e1 = __fsub_rn(__fsub_rn(t1, a1), y1);
         a1 = t1;
-        const float y2 = __fsub_rn(down[(long)m * ncell + t], e2);
+        const float y2 = __fsub_rn(down[o], e2);
         const float t2 = __fadd_rn(a2, y2);
         e2 = __fsub_rn(__fsub_rn(t2, a2), y2);
         a2 = t2;

@@ -129,3 +129,28 @@ class Engine:
                                                 whitecoe, int(nrec_div), int(inorm), ip_, lp, up,
                                                 dp, flags), "migrate_stack")
         return image, illum
+
+    def migrate_stack_windows(self, src_cells, win_x0, win_nx, seis, whitecoe: float,
+                              nrec_div: int, inorm: bool, image=None, illum=None,
+                              graph: bool = True):
+        """Stacked survey image [nz, nx] of shots with their own aperture
+        windows (interior columns [win_x0[i], win_x0[i]+win_nx[i])); sources
+        are flat cells of each shot's own padded grid."""
+        src = self._src(src_cells)
+        x0 = np.ascontiguousarray(win_x0, np.int32)
+        wn = np.ascontiguousarray(win_nx, np.int32)
+        p = self.prob
+        if image is None:
+            image = np.zeros((p.nz, p.nx), np.float32)
+        if illum is None:
+            illum = np.zeros((p.nz, p.nx), np.float32)
+        sp, sdev = _ptr(seis)
+        ip_, idev = _ptr(image)
+        lp, ldev = _ptr(illum)
+        assert sdev == idev == ldev, "mix of host and device buffers"
+        flags = (capi.RTM_DEVICE_PTRS if sdev else 0) | (0 if graph else capi.RTM_NO_GRAPH)
+        capi.check(capi.lib().rtm_migrate_stack_windows(self._h, len(src), capi.iptr(src),
+                                                        capi.iptr(x0), capi.iptr(wn), sp, whitecoe,
+                                                        int(nrec_div), int(inorm), ip_, lp, flags),
+                   "migrate_stack_windows")
+        return image, illum
