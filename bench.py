@@ -53,9 +53,17 @@ def parse():
     ap.add_argument("--nt", type=int, default=4000)
     ap.add_argument("--batch", type=int, default=0, help="shots per batch (0: all)")
     ap.add_argument("--coef", default="adaptive", choices=["adaptive", "taylor"])
+    ap.add_argument("--ring", default="f16", choices=["f32", "bf16", "f16"],
+                    help="boundary-ring storage (stencil and imaging stay FP32)")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip timing the plain single-shot drop-in for comparison")
     ap.add_argument("--cpu-sample-nt", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent"],
+                    help="stencil kernel form (auto: the autotuner picks it and shots per launch)")
+    ap.add_argument("--workload", default="multishot", choices=["multishot", "rvsp"],
+                    help="rvsp: batched uneven aperture windows, well receivers, autotuned")
     return ap.parse_args()
 
 
@@ -68,17 +76,21 @@ class Config:
         self.NT = a.nt
         self.nshot = a.shots
         self.coef = a.coef
+        self.ring = a.ring
         self.whitecoe = 1e-4
         # optimiser settings (the reference's parameter file: nthita=1000,
         # eps=1e-5, df=1; fmax = 2*f0)
         self.fmax, self.df, self.nthita, self.eps, self.nfdmin = 2 * self.f0, 1.0, 1000, 1e-5, 2
 
     def workload(self):
-        return {"workload": "multi-shot FP32 RTM %dx%d interior, 30-cell hybrid ABC, M=%d %s, "
-                            "%d steps, %d surface shots, full-spread receivers, Kahan stack"
-                            % (self.nz, self.nx, self.M, self.coef, self.NT, self.nshot),
+        return {"workload": "multi-shot RTM %dx%d interior, 30-cell hybrid ABC, M=%d %s "
+                            "coefficients, %d steps, %d surface shots, full-spread receivers, "
+                            "FP32 stencil/imaging, %s boundary rings, Kahan stack"
+                            % (self.nz, self.nx, self.M, self.coef, self.NT, self.nshot,
+                               self.ring.upper()),
                 "nz": self.nz, "nx": self.nx, "N2": self.N2, "M": self.M, "nt": self.NT,
-                "shots": self.nshot, "dx_m": self.h, "dt_s": self.tao, "coefficients": self.coef}
+                "shots": self.nshot, "dx_m": self.h, "dt_s": self.tao, "coefficients": self.coef,
+                "ring_storage": self.ring}
 
 
 def build_problems(cfg, dv=1.0):
@@ -208,6 +220,125 @@ def run_reference_arm(a, cfg):
     print(json.dumps(line))
 
 
+def rvsp_geometry(cfg, nshot=128, seed=1237, wmin=300, wmax=1201, well_x=600, z0=50, nrec=300):
+    """Reverse-VSP survey on the multi-shot model: nshot surface sources, each
+    with a seeded aperture window of width U[wmin, wmax] columns around it
+    that contains the well; nrec receivers down the well at interior column
+    well_x, depths z0 .. z0+nrec-1.  Returns (sources (z, x) in the survey's
+    padded grid, window starts, window widths, receiver line)."""
+    rng = np.random.default_rng(seed)
+    N2, nx = cfg.N2, cfg.nx
+    xs = np.linspace(0, nx - 1, nshot).round().astype(int)
+    w = rng.integers(wmin, min(wmax, nx) + 1, nshot)
+    xa = np.clip(xs - w // 2, np.maximum(0, well_x - w + 1), np.minimum(well_x, nx - w))
+    sx = np.clip(xs, xa, xa + w - 1)
+    src = [(N2 + 1, N2 + int(x)) for x in sx]
+    return src, xa.astype(np.int32), w.astype(np.int32), (N2 + z0, N2 + well_x, 1, 0, nrec)
+
+
+def run_rvsp(a, cfg):
+    """Batched uneven shots (reverse VSP): all shots' windows advance
+    together; kernel form and shots per launch from the autotuner; FP32."""
+    import torch
+    from rtm_gpu_gb300 import Engine, capi, synth
+    from rtm_gpu_gb300.problem import build_problem
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    nshot = a.shots if a.shots != 64 else 128
+    src, xa, wn, rec = rvsp_geometry(cfg, nshot=nshot)
+    vtrue = synth.model_c2(nz=cfg.nz, nx=cfg.nx)
+    vmig = synth.smooth_model(vtrue, 10.0)
+    table = None
+    if cfg.coef == "adaptive":
+        from rtm_gpu_gb300 import coeffs
+        table = coeffs.table_source(nfdmax=cfg.M, nfdmin=cfg.nfdmin, tao=cfg.tao, h=cfg.h,
+                                    fmax=cfg.fmax, df=cfg.df, nthita=cfg.nthita, eps=cfg.eps)
+    kw = dict(N2=cfg.N2, M=cfg.M, NT=cfg.NT, h=cfg.h, tao=cfg.tao, f0=cfg.f0,
+              adaptive=cfg.coef == "adaptive", compen=True, rec=rec, coef_table=table)
+    ptrue, pmig = build_problem(vtrue, **kw), build_problem(vmig, **kw)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    batch = a.batch or nshot
+    # observed data on the whole survey (true minus smoothed model)
+    full_src = [pmig.src_flat(z, x) for z, x in src]
+    seis = torch.zeros((nshot, pmig.nrec, pmig.NT), dtype=torch.float32, device="cuda")
+    tmp = torch.zeros_like(seis)
+    with Engine(ptrue, batch=min(batch, 64), stream=sh) as e:
+        e.model(full_src, out=seis)
+    with Engine(pmig, batch=min(batch, 64), stream=sh) as e:
+        e.model(full_src, out=tmp)
+    seis -= tmp
+    del tmp
+    # sources in each shot's own padded grid
+    wsrc = [z * (int(w) + 2 * cfg.N2) + (x - int(x0)) for (z, x), x0, w in zip(src, xa, wn)]
+    ring = {"f32": capi.RTM_RING_F32, "bf16": capi.RTM_RING_BF16, "f16": capi.RTM_RING_F16}[cfg.ring]
+    eng = Engine(pmig, batch=batch, stream=sh, ring_precision=ring)
+    tuned = None
+    if a.kernel == "auto":
+        tuned = eng.autotune(wsrc, xa, wn, nsteps=20)
+    else:
+        v = capi.RTM_KERNEL_TILED if a.kernel == "tiled" else capi.RTM_KERNEL_PERSISTENT
+        eng.set_kernel(v, v)
+    kern = eng.kernel()
+    img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
+    ill = torch.zeros_like(img)
+
+    def step():
+        eng.migrate_stack_windows(wsrc, xa, wn, seis, cfg.whitecoe, nshot, True, image=img, illum=ill)
+
+    for _ in range(max(3, a.warmup)):
+        step()
+    torch.cuda.synchronize()
+    eng.launches(reset=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks("/tmp/bench_clocks_rvsp.csv") as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(a.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    launches = eng.launches()
+    NZ = pmig.NZ
+    cu = sum(cfg.NT * (2 * NZ * (int(w) + 2 * cfg.N2) + cfg.nz * int(w)) for w in wn)
+    # end to end: gathers from pinned host memory, image back to the host
+    seis_h = seis.cpu().pin_memory()
+    img_h = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32).pin_memory()
+    ill_h = torch.zeros_like(img_h).pin_memory()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        eng.migrate_stack_windows(wsrc, xa, wn, seis_h, cfg.whitecoe, nshot, True, image=img_h,
+                                  illum=ill_h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / a.steps
+    line = {"metric": METRIC, "value": cu / (ms / 1e3) / 1e9, "unit": METRIC, "n_gpus": 1,
+            "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched uneven shots, reverse VSP: %dx%d model, %d surface "
+                                   "sources with aperture windows of 300-1201 columns, %d well "
+                                   "receivers at x=600, z=50..%d, %d steps, M=%d %s, %s rings"
+                                   % (cfg.nz, cfg.nx, nshot, rec[4], 50 + rec[4] - 1, cfg.NT,
+                                      cfg.M, cfg.coef, cfg.ring.upper()),
+                       "shots": nshot, "mean_window": float(np.mean(wn)), "batch": batch,
+                       "autotuned": {"fwd_kernel": ["tiled", "persistent"][kern["fwd"]],
+                                     "bwd_kernel": ["tiled", "persistent"][kern["bwd"]],
+                                     "shots_per_launch": kern["shots_per_launch"],
+                                     "tuning_gcells_per_s": tuned},
+                       "l2": "inputs larger than L2 (%.1f GB of wavefields and rings)"
+                             % (eng.device_bytes / 1e9)},
+            "shots_per_hour": nshot / (ms / 1e3) * 3600,
+            "e2e": {"value": cu / (ms_e2e / 1e3) / 1e9, "unit": METRIC,
+                    "h2d_bytes_per_step": int(seis_h.numel() * 4),
+                    "d2h_bytes_per_step": int((img_h.numel() + ill_h.numel()) * 4)},
+            "clocks": clk.summary(0), "gpu_launches": launches,
+            "gpu_launches_per_step": launches // a.steps}
+    print(json.dumps(line))
+    eng.close()
+
+
 def main():
     a = parse()
     cfg = Config(a)
@@ -215,6 +346,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if a.impl == "reference":
         run_reference_arm(a, cfg)
+        return
+    if a.workload == "rvsp":
+        run_rvsp(a, cfg)
         return
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -244,7 +378,16 @@ def main():
     del tmp
     torch.cuda.synchronize()
 
-    eng = Engine(pmig, batch=batch, stream=sh)
+    from rtm_gpu_gb300 import capi
+    ring = {"f32": capi.RTM_RING_F32, "bf16": capi.RTM_RING_BF16, "f16": capi.RTM_RING_F16}[cfg.ring]
+    eng = Engine(pmig, batch=batch, stream=sh, ring_precision=ring)
+    tuned = None
+    if a.kernel == "auto":
+        tuned = eng.autotune(src, nsteps=20)
+    else:
+        v = capi.RTM_KERNEL_TILED if a.kernel == "tiled" else capi.RTM_KERNEL_PERSISTENT
+        eng.set_kernel(v, v)
+    kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
 
@@ -269,7 +412,7 @@ def main():
         if dist:
             dist.barrier()
     ms = ev0.elapsed_time(ev1) / a.steps
-    launches = eng.launches() // a.steps
+    launches = eng.launches()  # kernels launched inside the timed region (all K steps)
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -299,7 +442,7 @@ def main():
            "d2h_bytes_per_step": int((img_h.numel() + ill_h.numel()) * 4)}
 
     # roofline of the dominant kernel (backward stencil) from a timed pass
-    nb = min(batch, nshot)
+    nb = min(kern["shots_per_launch"], nshot)  # shots of one launch
     eng.set_timing(True)
     r1d = torch.zeros((nb, pmig.NZ, pmig.NX), dtype=torch.float32, device="cuda")
     eng.migrate(src[:nb], seis[:nb], rel1=r1d, rel2=torch.zeros_like(r1d))
@@ -322,6 +465,23 @@ def main():
                 "pad_kernel_ms": tm["pad_ms"] / max(tm["pad_n"], 1),
                 "time_share": {"fwd": tm["fwd_ms"], "bwd": tm["bwd_ms"], "pad": tm["pad_ms"]}}
 
+    # the plain single-shot GPU drop-in (the reference's per-shot launch
+    # sequence on the rtm_k_* kernels) on one shot of the same workload
+    plain = None
+    if rank == 0 and not a.no_plain:
+        from rtm_gpu_gb300.engine import plain_migrate_shot
+        s0 = seis_h[0].numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plain_migrate_shot(pmig, src[0], s0)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        cu_shot = cell_updates_per_shot(pmig.nz, pmig.nx, pmig.N2, pmig.NT)
+        plain = {"seconds_per_shot": tp, "shots_per_hour": 3600.0 / tp,
+                 "value": cu_shot / tp / 1e9, "unit": METRIC,
+                 "what": "rtm_plain_migrate_shot: kernel.cu's per-shot loop on the rtm_k_* "
+                         "drop-in kernels, FP32 rings, host wall clock"}
+
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
         nt_s = a.cpu_sample_nt or 60
@@ -333,11 +493,19 @@ def main():
                 "steps": a.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(cfg.workload(), batch=batch,
+                               kernels={"fwd": ["tiled", "persistent"][kern["fwd"]],
+                                        "bwd": ["tiled", "persistent"][kern["bwd"]],
+                                        "shots_per_launch": kern["shots_per_launch"],
+                                        "chosen_by": "autotuner" if tuned is not None else "flag",
+                                        "tuning_gcells_per_s": tuned},
                                l2="inputs larger than L2 (%.1f GB of wavefields and rings)"
                                   % (eng.device_bytes / 1e9)),
                 "shots_per_hour": nshot * world / (ms / 1e3) * 3600,
+                "plain_dropin": plain,
+                "speedup_vs_plain_shots_per_hour": (nshot * world / (ms / 1e3) * 3600 /
+                                                    plain["shots_per_hour"]) if plain else None,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-                "gpu_launches": launches}
+                "gpu_launches": launches, "gpu_launches_per_step": launches // a.steps}
         print(json.dumps(line))
     eng.close()
     if dist:

@@ -160,6 +160,38 @@ int rtm_coeffs_optimise_fp64(const rtm_ls_settings *s, double vmin, double dv, i
 int rtm_ls_coefs_fp64(const double *r, const double *bb, const int *M, int n, double hzx,
                       double *c);
 
+/* Learned coefficients: a 3-layer MLP (3 -> 64 -> 64 -> 16, tanh, FP32)
+ * mapping (r = v*tao/h, band limit kmax*h, M) to c_1..c_M, trained on the GPU
+ * by its own forward/backward/Adam kernels on sets the FP64 optimiser makes.
+ * Parameters are a flat array of rtm_mlp_nparams() floats; the normalisation
+ * block is in_mean[3], in_scale[3], out_mean[16], out_scale[16].  Samples:
+ * x[n][3] = (r, kh, M), c[n][16] = c_1..c_16 (entries >= M ignored).  The
+ * training loss (rtm_mlp_grad, rtm_mlp_train) is the mean squared relative
+ * difference of the FD symbols of the network's and the sample's coefficients
+ * on 8 wavenumbers (kh/8 .. kh) x 4 angles (0 .. pi/4). */
+typedef struct rtm_mlp rtm_mlp;
+int rtm_mlp_create(rtm_mlp **m, unsigned seed);
+int rtm_mlp_destroy(rtm_mlp *m);
+int rtm_mlp_nparams(void);
+int rtm_mlp_get_params(const rtm_mlp *m, float *params);
+int rtm_mlp_set_params(rtm_mlp *m, const float *params);
+int rtm_mlp_set_norm(rtm_mlp *m, const float *norm);
+int rtm_mlp_get_norm(const rtm_mlp *m, float *norm);
+int rtm_mlp_grad(rtm_mlp *m, const float *x, const float *c, int n, float *grad, float *loss);
+int rtm_mlp_train(rtm_mlp *m, const float *x, const float *c, int n, int epochs, int batch,
+                  float lr, float *final_loss);
+int rtm_mlp_predict(rtm_mlp *m, const float *x, int n, float *c);
+/* Largest relative phase-velocity error |v_FD/v-1| of n coefficient sets
+ * c[n][cstride] over kh in (0,bb] (nk samples) and angles [0,pi/4] (nth+1). */
+int rtm_disp_error_fp64(const double *c, int cstride, const int *M, const double *r,
+                        const double *bb, int n, int nk, int nth, double hzx, double *err);
+/* Coefficient table (funMandC layout) from the network with length M for
+ * every needed bin; bins whose network set misses `tol` use the FP64
+ * optimiser's set instead (*nfallback counts them). */
+int rtm_coeffs_mlp(rtm_mlp *m, const rtm_ls_settings *s, double vmin, int nvel, const int *need,
+                   int M, double tol, int *len, int *index, float *coef, int ccap, int *nc,
+                   int *nfallback, double *err_net, double *err_used);
+
 /* ======================================================================
  * 3. Shot level.
  * ====================================================================== */
@@ -240,6 +272,14 @@ int rtm_migrate_stack_windows(rtm_ctx *ctx, int nshot, const int *src_cells, con
                               const int *win_nx, const float *seis, float whitecoe, int nrec_div,
                               int inorm, float *image, float *illum, int flags);
 
+/* The reference's per-shot loop (kernel.cu:798-933) on the rtm_k_* kernels
+ * (legacy stream, one synchronous copy of the trace samples per backward
+ * step, device buffers allocated inside): the plain single-shot drop-in.
+ * Receivers must form the reference's surface line (rdz == 0).  seis is
+ * trace-major [nrec][NT]; rel1/rel2 receive the padded grids [NZ][NX]. */
+int rtm_plain_migrate_shot(const rtm_problem *p, int src_cell, const float *seis, float *rel1,
+                           float *rel2);
+
 /* Per-launch timing: with timing enabled, launches go one by one (no graph)
  * with CUDA events around each kernel; rtm_ctx_timing returns the summed
  * milliseconds and launch counts of [0] forward stencil, [1] backward
@@ -248,6 +288,25 @@ int rtm_ctx_set_timing(rtm_ctx *ctx, int enable);
 int rtm_ctx_timing(const rtm_ctx *ctx, double ms[3], long n[3]);
 /* Kernels this context has launched (graph replays count their kernels). */
 int rtm_ctx_launches(rtm_ctx *ctx, long *count, int reset);
+
+/* Stencil kernel form and shots per launch (no reference counterpart: the
+ * reference launches one shot at a time).  RTM_KERNEL_TILED: one CTA per
+ * 128 x 16 tile of every shot; RTM_KERNEL_PERSISTENT (default): a fixed grid
+ * of resident CTAs walks the batch's tiles with a two-stage TMA pipeline.
+ * Set separately for the forward and the backward stencil; shots_per_launch
+ * in 1..max_batch (0: max_batch). */
+enum { RTM_KERNEL_TILED = 0, RTM_KERNEL_PERSISTENT = 1 };
+int rtm_ctx_set_kernel(rtm_ctx *ctx, int fwd_variant, int bwd_variant, int shots_per_launch);
+int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
+                       int *shots_per_launch);
+/* Autotuner: times nsteps forward and nsteps backward time steps of the
+ * first shots of a survey (optional windows as rtm_migrate_stack_windows)
+ * for each kernel form and for shots per launch max_batch, /2, /4, ...,
+ * keeps the fastest setting in the context and returns its rate in
+ * grid-cell updates per second (/1e9).  Wavefield contents are scratch
+ * afterwards. */
+int rtm_ctx_autotune(rtm_ctx *ctx, int nshot, const int *src_cells, const int *win_x0,
+                     const int *win_nx, int nsteps, double *gcells_per_s);
 
 #ifdef __cplusplus
 }

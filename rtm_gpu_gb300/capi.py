@@ -19,6 +19,7 @@ RTM_OK = 0
 RTM_DEVICE_PTRS = 1
 RTM_NO_GRAPH = 2
 RTM_RING_F32, RTM_RING_BF16, RTM_RING_F16 = 0, 1, 2
+RTM_KERNEL_TILED, RTM_KERNEL_PERSISTENT = 0, 1
 
 vp = C.c_void_p
 fp = C.POINTER(C.c_float)
@@ -68,7 +69,7 @@ def lib():
     """The loaded C-ABI library.  Raises if it has not been built."""
     global _lib
     if _lib is None:
-        path = _build.LIB
+        path = os.environ.get("RTM_GB300_LIB") or _build.LIB  # override: a library built elsewhere
         if not os.path.exists(path):
             raise RuntimeError(
                 "rtm_gpu_gb300: native library %s is missing; run "
@@ -92,9 +93,13 @@ def lib():
         L.rtm_migrate_batch.argtypes = [vp, I, ip, vp, vp, vp, I]
         L.rtm_migrate_stack.argtypes = [vp, I, ip, vp, F, I, I, vp, vp, vp, vp, I]
         L.rtm_migrate_stack_windows.argtypes = [vp, I, ip, ip, ip, vp, F, I, I, vp, vp, I]
+        L.rtm_plain_migrate_shot.argtypes = [C.POINTER(RtmProblem), I, fp, fp, fp]
         L.rtm_ctx_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_long)]
         L.rtm_ctx_set_timing.argtypes = [vp, I]
         L.rtm_ctx_launches.argtypes = [vp, C.POINTER(C.c_long), I]
+        L.rtm_ctx_set_kernel.argtypes = [vp, I, I, I]
+        L.rtm_ctx_get_kernel.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.rtm_ctx_autotune.argtypes = [vp, I, ip, ip, ip, I, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 

@@ -29,7 +29,7 @@
 namespace {
 
 constexpr double kPi = 3.1415926535898;  // LSMOrCon_rec_2D.cpp:4
-constexpr int kMaxM = 16;
+constexpr int kMaxM = 16;  // rtm_ls_coefs_fp64 writes c[i*(kMaxM+1) + l]
 constexpr int kThreads = 128;
 
 __constant__ double c_gl_t[5] = {-0.9061798459, -0.5384693101, 0.0, 0.5384693101, 0.9061798459};

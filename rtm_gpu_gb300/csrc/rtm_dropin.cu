@@ -7,6 +7,7 @@
 // ring cells only instead of the full grid; the rotation kernels are plain
 // vectorisable copies.  No allocation happens here.
 #include <cstdio>
+#include <vector>
 
 #include "rtm_common.cuh"
 
@@ -432,3 +433,148 @@ int rtm_k_Rel_Compen(float *DBW2, float *DFW2, float *DBWADD, float *DFWADD, flo
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// The reference's per-shot loop (kernel.cu:798-933) on the drop-in kernels:
+// 5 launches per forward step, 8 launches and one synchronous host-to-device
+// copy of the step's trace samples per backward step, on the legacy default
+// stream -- the "plain single-shot GPU drop-in" the batched engine is
+// measured against.  Host inputs/outputs; device buffers are allocated and
+// freed here.  The receivers are the problem's line (rdz == 0).
+namespace {
+
+template <class T>
+struct DevArr {
+    T *p = nullptr;
+    ~DevArr()
+    {
+        if (p) cudaFree(p);
+    }
+    int alloc(size_t n)
+    {
+        if (cudaMalloc(&p, sizeof(T) * (n ? n : 1)) != cudaSuccess) {
+            cudaGetLastError();
+            rtm_set_last_error("cudaMalloc failed");
+            return RTM_ERR_NOMEM;
+        }
+        cudaMemset(p, 0, sizeof(T) * (n ? n : 1));
+        return RTM_OK;
+    }
+};
+
+}  // namespace
+
+extern "C" int rtm_plain_migrate_shot(const rtm_problem *p, int src_cell, const float *seis,
+                                      float *rel1, float *rel2)
+{
+    if (!p || !seis || !rel1 || !rel2 || p->rdz != 0 || p->rdx < 1 || p->nrec < 1) return RTM_ERR_ARG;
+    const int N2 = p->N2, M = p->M, NT = p->NT;
+    const int NZ = p->nz + 2 * N2, NX = p->nx + 2 * N2, nz = p->nz, nx = p->nx;
+    if (int rc = check_grid(NZ, NX, N2, M)) return rc;
+    const long nxz = (long)NZ * NX;
+    const size_t gb = sizeof(float) * nxz;
+    const int r_u = src_cell / NX, r_x = src_cell % NX;
+    const int s_l = p->rx0, s_z = p->rz0, ds = p->rdx, n = p->nrec, s_r = (n - 1) * ds + s_l;
+    DevArr<float> FW0, FW1, FW2, FWb, BW0, BW1, BW2, FA, BA, R1, R2, v, r1, w, c, lf, rt, up, dw, sd;
+    DevArr<int> idx;
+    int rc;
+    DevArr<float> *g[] = {&FW0, &FW1, &FW2, &FWb, &BW0, &BW1, &BW2, &FA, &BA, &R1, &R2, &v, &r1};
+    for (auto *a : g)
+        if ((rc = a->alloc(nxz))) return rc;
+    const int nc = p->adaptive ? p->index[p->nbins] : M + 1;
+    if ((rc = w.alloc(N2 + 1)) || (rc = c.alloc(nc)) || (rc = idx.alloc(p->adaptive ? p->nbins + 1 : 1)) ||
+        (rc = lf.alloc((size_t)M * nz * NT)) || (rc = rt.alloc((size_t)M * nz * NT)) ||
+        (rc = up.alloc((size_t)M * nx * NT)) || (rc = dw.alloc((size_t)M * nx * NT)) ||
+        (rc = sd.alloc(n)))
+        return rc;
+    RTM_CUDA_TRY(cudaMemcpy(v.p, p->v, gb, cudaMemcpyHostToDevice));
+    RTM_CUDA_TRY(cudaMemcpy(r1.p, p->r1, gb, cudaMemcpyHostToDevice));
+    RTM_CUDA_TRY(cudaMemcpy(w.p, p->w, sizeof(float) * (N2 + 1), cudaMemcpyHostToDevice));
+    RTM_CUDA_TRY(cudaMemcpy(c.p, p->coef, sizeof(float) * nc, cudaMemcpyHostToDevice));
+    if (p->adaptive)
+        RTM_CUDA_TRY(cudaMemcpy(idx.p, p->index, sizeof(int) * (p->nbins + 1), cudaMemcpyHostToDevice));
+    const float spike = p->spike;
+    RTM_CUDA_TRY(cudaMemcpy(FW1.p + (long)r_u * NX + r_x, &spike, sizeof(float), cudaMemcpyHostToDevice));
+    const float tao2 = p->tao2, h2 = p->h2, vmin = p->vmin, dv = p->dv, hzx2_1 = p->hzx2_1;
+    const float taoh = p->taoh, taoh2 = p->taoh2;
+#define TRYK(x)                      \
+    do {                             \
+        if ((rc = (x)) != RTM_OK) return rc; \
+    } while (0)
+    TRYK(rtm_k_Equal(lf.p, rt.p, up.p, dw.p, FW0.p, FW1.p, NZ, NX, N2, M, nullptr));
+    for (int k = 2; k < NT; ++k) {
+        const float wav = (k < p->NT2) ? p->wav[k - 1] : 0.0f;
+        if (p->adaptive)
+            TRYK(rtm_k_Add(v.p, FW2.p, FW0.p, FW1.p, c.p, idx.p, tao2, h2, vmin, dv, M, NZ, NX, (int)nxz,
+                           r_u, r_x, wav, hzx2_1, nullptr));
+        else
+            TRYK(rtm_k_Add_Con(v.p, FW2.p, FW0.p, FW1.p, c.p, tao2, h2, M, NZ, NX, (int)nxz, r_u, r_x, wav,
+                               hzx2_1, nullptr));
+        TRYK(rtm_k_Hybrid1(FW1.p, FW0.p, FW2.p, FWb.p, lf.p, rt.p, up.p, dw.p, v.p, r1.p, w.p, NZ, NX, N2,
+                           M, k, taoh, taoh2, nullptr));
+        TRYK(rtm_k_Hybrid2(FW1.p, FW0.p, FW2.p, FWb.p, lf.p, rt.p, up.p, dw.p, v.p, r1.p, w.p, NZ, NX, N2,
+                           M, k, taoh, taoh2, nullptr));
+        TRYK(rtm_k_Hybrid3(FW1.p, FW0.p, FW2.p, FWb.p, lf.p, rt.p, up.p, dw.p, v.p, r1.p, w.p, NZ, NX, N2,
+                           M, k, taoh, taoh2, nullptr));
+        TRYK(rtm_k_Deliver(FW1.p, FW0.p, FW2.p, NZ, NX, nullptr));
+    }
+    // hand-off (kernel.cu:822-825) and image initialisation (:859-885)
+    RTM_CUDA_TRY(cudaMemcpy(BW0.p, FW1.p, gb, cudaMemcpyDeviceToDevice));
+    RTM_CUDA_TRY(cudaMemcpy(BW1.p, FW0.p, gb, cudaMemcpyDeviceToDevice));
+    {
+        std::vector<float> b0(nxz), b1(nxz), m1(nxz), m2(nxz), ba(nxz, 0.0f), fa(nxz, 0.0f);
+        RTM_CUDA_TRY(cudaMemcpy(b0.data(), BW0.p, gb, cudaMemcpyDeviceToHost));
+        RTM_CUDA_TRY(cudaMemcpy(b1.data(), BW1.p, gb, cudaMemcpyDeviceToHost));
+        const long src = (long)r_u * NX + r_x;
+        for (long i = 0; i < nxz; ++i) {
+            const float h0 = 0.0f, h1 = (i == src) ? spike : 0.0f;
+            if (p->compen) {
+                ba[i] = b0[i] + b1[i];
+                fa[i] = h0 + h1;
+                m1[i] = fa[i] * ba[i] + h0 * b0[i];
+            } else {
+                m1[i] = h1 * b1[i] + h0 * b0[i];
+            }
+            m2[i] = b1[i] * b1[i] + b0[i] * b0[i];
+        }
+        RTM_CUDA_TRY(cudaMemcpy(R1.p, m1.data(), gb, cudaMemcpyHostToDevice));
+        RTM_CUDA_TRY(cudaMemcpy(R2.p, m2.data(), gb, cudaMemcpyHostToDevice));
+        RTM_CUDA_TRY(cudaMemcpy(BA.p, ba.data(), gb, cudaMemcpyHostToDevice));
+        RTM_CUDA_TRY(cudaMemcpy(FA.p, fa.data(), gb, cudaMemcpyHostToDevice));
+        RTM_CUDA_TRY(cudaMemcpy(FW2.p, fa.data(), gb, cudaMemcpyHostToDevice));
+        RTM_CUDA_TRY(cudaMemset(FW0.p, 0, gb));
+        RTM_CUDA_TRY(cudaMemset(FW1.p, 0, gb));
+        RTM_CUDA_TRY(cudaMemset(FWb.p, 0, gb));
+    }
+    std::vector<float> cs(n);
+    for (int k = NT - 3; k >= 0; --k) {
+        const float wav = (k < p->NT2) ? p->wav[k + 1] : 0.0f;
+        TRYK(rtm_k_BKEqual(lf.p, rt.p, up.p, dw.p, BW1.p, NZ, NX, N2, M, k, nullptr));
+        if (p->adaptive)
+            TRYK(rtm_k_BKAdd_EFF(v.p, BW2.p, BW0.p, BW1.p, c.p, idx.p, tao2, h2, vmin, dv, N2, NZ, NX,
+                                 (int)nxz, r_u, r_x, wav, hzx2_1, nullptr));
+        else
+            TRYK(rtm_k_BKAdd_EFF_Con(v.p, BW2.p, BW0.p, BW1.p, c.p, tao2, h2, N2, NZ, NX, (int)nxz, r_u,
+                                     r_x, M, wav, hzx2_1, nullptr));
+        TRYK(rtm_k_Deliver_EFF(BW1.p, BW0.p, BW2.p, N2, NZ, NX, nullptr));
+        for (int j = 0; j < n; ++j) cs[j] = seis[(long)j * NT + k + 1];
+        RTM_CUDA_TRY(cudaMemcpy(sd.p, cs.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+        if (p->adaptive)
+            TRYK(rtm_k_BKAdd(v.p, FW2.p, FW1.p, FW0.p, c.p, idx.p, sd.p, tao2, h2, vmin, dv, M, NZ, NX,
+                             (int)nxz, s_l, s_r, s_z, ds, hzx2_1, nullptr));
+        else
+            TRYK(rtm_k_BKAdd_Con(v.p, FW2.p, FW1.p, FW0.p, c.p, sd.p, tao2, h2, M, NZ, NX, (int)nxz, s_l,
+                                 s_r, s_z, ds, hzx2_1, nullptr));
+        TRYK(rtm_k_BKHybrid1(FW1.p, FW0.p, FW2.p, FWb.p, v.p, r1.p, w.p, NZ, NX, N2, taoh, taoh2, nullptr));
+        TRYK(rtm_k_BKHybrid2(FW1.p, FW0.p, FW2.p, FWb.p, v.p, r1.p, w.p, NZ, NX, N2, taoh, taoh2, nullptr));
+        TRYK(rtm_k_Deliver(FW1.p, FW0.p, FW2.p, NZ, NX, nullptr));
+        if (p->compen)
+            TRYK(rtm_k_Rel_Compen(FW2.p, BW2.p, FA.p, BA.p, R1.p, R2.p, NZ, NX, nullptr));
+        else
+            TRYK(rtm_k_Rel_NonCompen(FW2.p, BW2.p, R1.p, R2.p, NZ, NX, nullptr));
+    }
+#undef TRYK
+    RTM_CUDA_TRY(cudaMemcpy(rel1, R1.p, gb, cudaMemcpyDeviceToHost));
+    RTM_CUDA_TRY(cudaMemcpy(rel2, R2.p, gb, cudaMemcpyDeviceToHost));
+    return RTM_OK;
+}

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "rtm_engine_kernels.cuh"
@@ -72,6 +73,7 @@ struct rtm_ctx {
     int nbins = 1;
     // device
     float *v = nullptr, *r1 = nullptr, *w = nullptr, *ctab = nullptr;
+    float4 *ctab4 = nullptr;  // adaptive table in float4 groups
     int4 *pad_meta = nullptr;
     float4 *pad_fac = nullptr;
     float *S[3] = {nullptr, nullptr, nullptr}, *R[3] = {nullptr, nullptr, nullptr};
@@ -93,7 +95,11 @@ struct rtm_ctx {
     // per-shot geometry of the current batch (device): padded width, window
     // start column in the survey interior, receiver start column
     int *gnx = nullptr, *gxa = nullptr, *grx0 = nullptr;
+    int *gitem = nullptr;              // [B+1] first tile item of each shot (persistent kernel)
     std::vector<int> hnx, hxa;         // host copies for the current batch
+    int kv[2] = {RTM_KERNEL_PERSISTENT, RTM_KERNEL_PERSISTENT};  // stencil kernel form (fwd, bwd)
+    int nbl = 0;                           // shots per launch (<= B)
+    int kstop = 0;                         // autotuning: time steps per phase (0: all)
     bool windowed = false;             // current batch uses per-shot models
     float *vs = nullptr, *r1s = nullptr;          // [B][NZ][P] window models
     int4 *meta_s = nullptr;
@@ -138,7 +144,8 @@ void free_all(rtm_ctx *c)
     for (float *p : fl)
         if (p) cudaFree(p);
     if (c->src) cudaFree(c->src);
-    for (int *q : {c->gnx, c->gxa, c->grx0})
+    if (c->ctab4) cudaFree(c->ctab4);
+    for (int *q : {c->gnx, c->gxa, c->grx0, c->gitem})
         if (q) cudaFree(q);
     if (c->vs) cudaFree(c->vs);
     if (c->r1s) cudaFree(c->r1s);
@@ -166,13 +173,28 @@ struct StepMaps {
     const CUtensorMap *A, *S, *A0, *S0;
 };
 
+// grid of the persistent stencil kernel: resident CTAs per SM x SMs
+template <int MMAX, bool AD, int MODE>
+int &pipe_grid()
+{
+    static int g = 0;
+    return g;
+}
+
 template <int MMAX, bool AD, int MODE>
 int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb)
 {
+    const CUtensorMap &fv = c->windowed ? c->flatVs : c->flatV;
+    if (c->kv[MODE] == RTM_KERNEL_PERSISTENT) {
+        const unsigned smem = eng::PipeSmem<MMAX, MODE>::BYTES;
+        eng::k_step_pipe<MMAX, AD, MODE><<<pipe_grid<MMAX, AD, MODE>(), eng::NTHREADS, smem, c->st>>>(
+            *m.A, *m.S, *m.A0, *m.S0, fv, c->imaps, a, c->gitem, nb);
+        return RTM_OK;
+    }
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
-    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(*m.A, *m.S, *m.A0, *m.S0,
-                                                                      c->windowed ? c->flatVs : c->flatV, c->imaps, a);
+    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
+                                                                      c->imaps, a);
     return RTM_OK;
 }
 
@@ -181,6 +203,13 @@ void set_attr_t()
 {
     const int smem = (int)eng::Smem<MMAX, MODE>::BYTES;
     cudaFuncSetAttribute(eng::k_step<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int psmem = (int)eng::PipeSmem<MMAX, MODE>::BYTES;
+    cudaFuncSetAttribute(eng::k_step_pipe<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem);
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, eng::k_step_pipe<MMAX, AD, MODE>, eng::NTHREADS, psmem);
+    pipe_grid<MMAX, AD, MODE>() = std::max(1, occ) * std::max(1, sms);
 }
 
 template <int MMAX>
@@ -194,12 +223,12 @@ void set_attr_m()
 
 void init_step_attrs()
 {
-    static bool done = false;
-    if (done) return;
-    set_attr_m<4>();
-    set_attr_m<8>();
-    set_attr_m<12>();
-    done = true;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        set_attr_m<4>();
+        set_attr_m<8>();
+        set_attr_m<12>();
+    });
 }
 
 template <int MMAX>
@@ -231,7 +260,7 @@ eng::StepArgs base_step(rtm_ctx *c)
     a.vmin = c->p.vmin; a.dv = c->p.dv; a.tao2 = c->p.tao2; a.h2 = c->p.h2;
     a.k0 = (float)(1.0 + (double)c->p.hzx2_1);
     a.hzx2_1 = c->p.hzx2_1;
-    a.v = c->v; a.ctab = c->ctab; a.src = c->src; a.compen = c->p.compen;
+    a.v = c->v; a.ctab = c->ctab; a.ctab4 = c->ctab4; a.src = c->src; a.compen = c->p.compen;
     a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = 0;
     a.rel1 = c->rel1; a.rel2 = c->rel2; a.sacc = c->sacc; a.racc = c->racc;
     a.nxs = c->gnx; a.rx0s = c->grx0; a.vshot = c->windowed ? 1 : 0;
@@ -241,7 +270,7 @@ eng::StepArgs base_step(rtm_ctx *c)
 eng::PadArgs base_pad(rtm_ctx *c)
 {
     eng::PadArgs a{};
-    a.NZ = c->NZ; a.P = c->P; a.N2 = c->N2;
+    a.NZ = c->NZ; a.P = c->P; a.N2 = c->N2; a.M = c->M;
     a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
     a.nxs = c->gnx; a.rx0s = c->grx0;
     a.meta = c->windowed ? c->meta_s : c->pad_meta;
@@ -312,7 +341,8 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     eng::StepArgs sa = base_step(c);
     eng::PadArgs pa = base_pad(c);
     const long npad = abc_count(c->NZ, c->NX, c->N2) + (rec_on ? c->nrec : 0) + (r16 ? c->ringsz : 0);
-    for (int k = 2; k < NT; ++k) {
+    const int kend = c->kstop ? std::min(c->kstop, NT) : NT;  // kstop-2 steps when tuning
+    for (int k = 2; k < kend; ++k) {
         float *a0 = c->S[(k - 2) % 3], *a1 = c->S[(k - 1) % 3], *a2 = c->S[k % 3];
         sa.a0 = a0; sa.a2 = a2; sa.pre = c->pre;
         sa.wavelet = (k < c->p.NT2) ? c->wav[k - 1] : 0.0f;
@@ -362,7 +392,8 @@ int enqueue_backward(rtm_ctx *c, int nb)
     sa.dstride = (long long)NT * c->nrec;
     eng::PadArgs pa = base_pad(c);
     const long npad = abc_count(c->NZ, c->NX, c->N2);
-    for (int k = NT - 3; k >= 0; --k) {
+    const int kend = c->kstop ? std::max(NT - c->kstop, 0) : 0;  // kstop-2 steps when tuning
+    for (int k = NT - 3; k >= kend; --k) {
         const int i2 = k % 3, i1 = (k + 1) % 3, i0 = (k + 2) % 3;
         sa.a0 = c->R[i0]; sa.a2 = c->R[i2]; sa.pre = c->pre;
         sa.s0 = c->S[i0]; sa.s2 = c->S[i2];
@@ -458,6 +489,10 @@ int set_batch(rtm_ctx *c, int nb, const int *src_cells, const int *xa, const int
         }
     }
     std::vector<int> hn(c->hnx);
+    std::vector<int> items(nb + 1, 0);  // tile items per shot: tile rows x tile columns
+    for (int i = 0; i < nb; ++i)
+        items[i + 1] = items[i] + cdiv(c->NZ, eng::TZ) * cdiv(c->hnx[i], eng::TX);
+    RTM_CUDA_TRY(cudaMemcpyAsync(c->gitem, items.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, c->st));
     RTM_CUDA_TRY(cudaMemcpyAsync(c->src, src_cells, sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
     RTM_CUDA_TRY(cudaMemcpyAsync(c->gnx, hn.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
     RTM_CUDA_TRY(cudaMemcpyAsync(c->gxa, c->hxa.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->st));
@@ -552,6 +587,7 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     c->NZ = p->nz + 2 * p->N2; c->NX = p->nx + 2 * p->N2;
     c->P = (c->NX + eng::TX - 1) / eng::TX * eng::TX;
     c->B = max_batch;
+    c->nbl = max_batch;
     c->nrec = p->nrec;
     c->ss = (long long)c->NZ * c->P;
     c->ringsz = 2L * c->M * (c->nx + c->nz);
@@ -618,6 +654,28 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     TRY(dalloc(c, &c->r1, grid));
     TRY(dalloc(c, &c->w, (size_t)c->N2 + 1));
     TRY(dalloc(c, &c->ctab, tab.size()));
+    if (p->adaptive) {
+        // float4 groups: ctab4[q][bin] = c_{4q..4q+3}
+        const int Q = (c->MM + 4) / 4;
+        std::vector<float4> t4((size_t)Q * c->nbins);
+        for (int q = 0; q < Q; ++q)
+            for (int b = 0; b < c->nbins; ++b) {
+                float g[4];
+                for (int k = 0; k < 4; ++k) {
+                    const int l = 4 * q + k;
+                    g[k] = l <= c->MM ? tab[(size_t)l * c->nbins + b] : 0.0f;
+                }
+                t4[(size_t)q * c->nbins + b] = make_float4(g[0], g[1], g[2], g[3]);
+            }
+        TRY(dalloc(c, &c->ctab4, t4.size()));
+        if (cudaMemcpy(c->ctab4, t4.data(), sizeof(float4) * t4.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            rtm_set_last_error("upload failed");
+            free_all(c);
+            delete c;
+            return RTM_ERR_CUDA;
+        }
+    }
     for (int i = 0; i < 3; ++i) {
         TRY(dalloc(c, &c->S[i], bgrid));
         TRY(dalloc(c, &c->R[i], bgrid));
@@ -640,6 +698,7 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     TRY(dalloc(c, &c->stage, (size_t)c->B * c->NT * std::max(c->nrec, 1)));
     TRY(dalloc(c, &c->src, (size_t)c->B));
     TRY(dalloc(c, &c->gnx, (size_t)c->B));
+    TRY(dalloc(c, &c->gitem, (size_t)c->B + 1));
     TRY(dalloc(c, &c->gxa, (size_t)c->B));
     TRY(dalloc(c, &c->grx0, (size_t)c->B));
     TRY(dalloc(c, &c->imax, (size_t)c->B));
@@ -702,8 +761,7 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
                 const float vc = p->v[ci], vq = p->v[q];
                 fac[t] = make_float4(taoh * vc, 1.0f / (taoh * vc + 1.0f), taoh2 * vq * vq, wj);
             }
-            const long ri = c->M > 0 ? eng::ring_index(z, x, NZ, NX, N2, c->M, c->nz, c->nx) : -1;
-            meta[t] = make_int4(z, x, kind | ((dz > 0 ? 1 : 2) << 2) | ((dx > 0 ? 1 : 2) << 4), (int)ri);
+            meta[t] = eng::pad_meta(t, NZ, NX, c->P, N2, c->M);
         }
         TRY(dalloc(c, &c->pad_meta, (size_t)nabc));
         TRY(dalloc(c, &c->pad_fac, (size_t)nabc));
@@ -772,6 +830,90 @@ int rtm_ctx_timing(const rtm_ctx *c, double ms[3], long n[3])
     return RTM_OK;
 }
 
+int rtm_ctx_set_kernel(rtm_ctx *c, int fwd_variant, int bwd_variant, int shots_per_launch)
+{
+    auto ok = [](int v) { return v == RTM_KERNEL_TILED || v == RTM_KERNEL_PERSISTENT; };
+    if (!c || !ok(fwd_variant) || !ok(bwd_variant) || shots_per_launch < 0 || shots_per_launch > c->B)
+        return RTM_ERR_ARG;
+    if (fwd_variant != c->kv[0] || bwd_variant != c->kv[1]) {
+        // captured graphs embed the old kernels
+        for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+        c->graphs.clear();
+        c->graph_kernels.clear();
+    }
+    c->kv[0] = fwd_variant;
+    c->kv[1] = bwd_variant;
+    c->nbl = shots_per_launch ? shots_per_launch : c->B;
+    return RTM_OK;
+}
+
+int rtm_ctx_get_kernel(const rtm_ctx *c, int *fwd_variant, int *bwd_variant, int *shots_per_launch)
+{
+    if (!c || !fwd_variant || !bwd_variant || !shots_per_launch) return RTM_ERR_ARG;
+    *fwd_variant = c->kv[0];
+    *bwd_variant = c->kv[1];
+    *shots_per_launch = c->nbl;
+    return RTM_OK;
+}
+
+int rtm_ctx_autotune(rtm_ctx *c, int nshot, const int *src_cells, const int *win_x0, const int *win_nx,
+                     int nsteps, double *gcells_per_s)
+{
+    if (!c || nshot < 1 || !src_cells || nsteps < 1 || (!win_x0) != (!win_nx)) return RTM_ERR_ARG;
+    nsteps = std::min(nsteps, c->NT - 3);  // both loops stay inside their step ranges
+    if (nsteps < 1) return RTM_ERR_ARG;
+    const bool was_timing = c->timing;
+    c->timing = false;
+    cudaEvent_t e[3];
+    for (auto &x : e) RTM_CUDA_TRY(cudaEventCreate(&x));
+    double best = -1.0;
+    int bf = c->kv[0], bb = c->kv[1], bn = c->nbl;
+    int rc = RTM_OK;
+    for (int nb = std::min(c->B, nshot); nb >= 1 && rc == RTM_OK; nb = nb > 4 ? nb / 2 : 0) {
+        if ((rc = set_batch(c, nb, src_cells, win_x0, win_nx))) break;
+        double cells = 0;  // cell updates of one forward + one backward step of the batch
+        for (int i = 0; i < nb; ++i)
+            cells += (double)c->NZ * c->hnx[i] + (double)c->nz * (c->hnx[i] - 2 * c->N2);
+        double fwd_ms[2], bwd_ms[2];
+        for (int v = 0; v < 2 && rc == RTM_OK; ++v) {
+            c->kv[0] = c->kv[1] = v;
+            c->kstop = 2 + 1;  // warm-up: one step of each phase
+            if ((rc = enqueue_forward(c, nb, false)) || (rc = enqueue_backward(c, nb))) break;
+            c->kstop = 2 + nsteps;
+            cudaEventRecord(e[0], c->st);
+            if ((rc = enqueue_forward(c, nb, false))) break;
+            cudaEventRecord(e[1], c->st);
+            if ((rc = enqueue_backward(c, nb))) break;
+            cudaEventRecord(e[2], c->st);
+            if (cudaEventSynchronize(e[2]) != cudaSuccess) { rc = RTM_ERR_CUDA; break; }
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, e[0], e[1]);
+            cudaEventElapsedTime(&b, e[1], e[2]);
+            fwd_ms[v] = a;
+            bwd_ms[v] = b;
+        }
+        if (rc) break;
+        const int vf = fwd_ms[1] < fwd_ms[0] ? 1 : 0, vb = bwd_ms[1] < bwd_ms[0] ? 1 : 0;
+        const double rate = cells * nsteps / ((fwd_ms[vf] + bwd_ms[vb]) * 1e-3) / 1e9;
+        if (rate > best) {
+            best = rate;
+            bf = vf; bb = vb; bn = nb;
+        }
+    }
+    c->kstop = 0;
+    c->timing = was_timing;
+    for (auto &x : e) cudaEventDestroy(x);
+    if (rc) return rc;
+    unsigned derr = 0;
+    rtm_device_error(&derr);
+    if (derr) {
+        rtm_set_last_error("device-side wait timed out");
+        return RTM_ERR_DEVICE;
+    }
+    if (gcells_per_s) *gcells_per_s = best;
+    return rtm_ctx_set_kernel(c, bf, bb, bn);
+}
+
 int rtm_ctx_launches(rtm_ctx *c, long *count, int reset)
 {
     if (!c || !count) return RTM_ERR_ARG;
@@ -785,8 +927,8 @@ int rtm_model_batch(rtm_ctx *c, int nshot, const int *src_cells, float *rec, int
     if (!c || nshot < 0 || (nshot > 0 && (!src_cells || !rec))) return RTM_ERR_ARG;
     const bool dev = flags & RTM_DEVICE_PTRS;
     const long long per = (long long)c->NT * c->nrec;
-    for (int s0 = 0; s0 < nshot; s0 += c->B) {
-        const int nb = std::min(c->B, nshot - s0);
+    for (int s0 = 0; s0 < nshot; s0 += c->nbl) {
+        const int nb = std::min(c->nbl, nshot - s0);
         if (int rc = set_batch(c, nb, src_cells + s0, nullptr, nullptr)) return rc;
         if (int rc = run_phase(c, 0, nb, flags)) return rc;
         if (c->nrec > 0) {
@@ -826,8 +968,8 @@ int rtm_migrate_batch(rtm_ctx *c, int nshot, const int *src_cells, const float *
     if (!c || nshot < 0 || (nshot > 0 && (!src_cells || (!seis && c->nrec > 0)))) return RTM_ERR_ARG;
     const bool dev = flags & RTM_DEVICE_PTRS;
     const long long gsz = (long long)c->NZ * c->NX;
-    for (int s0 = 0; s0 < nshot; s0 += c->B) {
-        const int nb = std::min(c->B, nshot - s0);
+    for (int s0 = 0; s0 < nshot; s0 += c->nbl) {
+        const int nb = std::min(c->nbl, nshot - s0);
         if (int rc = migrate_group(c, s0, nb, src_cells, nullptr, nullptr, seis, flags)) return rc;
         if (rel1)
             if (int rc = copy_grid_out(c, c->rel1, rel1 + s0 * gsz, nb, dev)) return rc;
@@ -854,8 +996,8 @@ static int migrate_stack_impl(rtm_ctx *c, int nshot, const int *src_cells, const
     const long ncell = (long)c->nz * c->nx;  // survey interior
     for (float *q : {c->ks1, c->kc1, c->ks2, c->kc2})
         RTM_CUDA_TRY(cudaMemsetAsync(q, 0, sizeof(float) * ncell, c->st));
-    for (int s0 = 0; s0 < nshot; s0 += c->B) {
-        const int nb = std::min(c->B, nshot - s0);
+    for (int s0 = 0; s0 < nshot; s0 += c->nbl) {
+        const int nb = std::min(c->nbl, nshot - s0);
         if (int rc = migrate_group(c, s0, nb, src_cells, xa, nx, seis, flags)) return rc;
         RTM_CUDA_TRY(cudaMemsetAsync(c->imax, 0, sizeof(unsigned) * nb, c->st));
         eng::k_illum_max<<<dim3(64, nb), 256, 0, c->st>>>(c->rel2, c->imax, c->ss, c->NZ, c->gnx,

@@ -7,20 +7,27 @@
 //     contiguous, so a batch is one 3-D tensor {NX, NZ, B} (row stride P)
 //     that one TMA descriptor covers;
 //   * the model (v, r_1) is one [NZ][P] grid shared by the batch;
-//   * coefficients: one coefficient-major table ctab[(l)*nbins + bin],
+//   * coefficients: one coefficient-major table of float4 groups
+//     ctab4[q*nbins + bin] = (c_4q .. c_4q+3) of velocity bin `bin`,
 //     zero-padded to the compile-time operator length MMAX, so every cell runs
-//     the same unrolled loop (adding 0*x leaves a sum unchanged);
+//     the same unrolled loop (adding 0*x leaves a sum unchanged) and gathers
+//     its M+1 coefficients with ceil((MMAX+1)/4) 16-byte loads;
 //   * boundary rings: [shot][NT][ring] with ring = 2M(nx+nz) cells
 //     (top band M*nx, bottom band M*nx, left band M*nz, right band M*nz).
 //
 // One time step of a batch is two launches:
-//   k_step  : the 2M-order update of every cell, u1 staged in shared memory by
-//             one TMA box per tile (halo included), z-neighbours streamed
-//             through a register queue, x-neighbours read as 128-bit shared
-//             loads.  Pad cells write their pre-blend value to `pre`, interior
-//             cells write the result.  The backward variant also advances the
-//             reconstructed source field on the interior and updates the
-//             imaging accumulators of every interior cell in the same pass.
+//   k_step  : the 2M-order update of every cell of a 128 x 16 tile.  Every
+//             input is staged in shared memory by TMA (a halo box for the
+//             field being advanced, flat tiles for u_{k-2}, v and the imaging
+//             accumulators); each lane owns one column, streams z-neighbours
+//             through a register queue and reads x-neighbours as
+//             conflict-free 32-bit shared loads.  Pad cells write their
+//             pre-blend value to `pre`, interior cells write the result.  The
+//             forward variant computes two rows per loop step; the backward
+//             variant advances the reconstructed source field and the
+//             receiver field in lockstep (one coefficient gather per cell
+//             serves both) and updates the imaging accumulators of every
+//             interior cell in the same pass.
 //   k_pad   : one-way update + blend of every pad cell (reading pre-blend
 //             values from `pre`), ring save (forward) or ring restore of the
 //             source field (backward), receiver recording (forward).
@@ -77,7 +84,8 @@ struct StepArgs {
     long long ss;              // floats between consecutive shots
     float vmin, dv, tao2, h2, k0, hzx2_1;
     const float *v;            // [NZ][P]
-    const float *ctab;         // [(MMAX+1)][nbins]
+    const float *ctab;         // fixed coefficients c[0..MMAX] (nbins == 1)
+    const float4 *ctab4;       // [ceil((MMAX+1)/4)][nbins] coefficient groups (adaptive)
     const float *a0;           // field A (u forward / R backward), level k-2
     float *a2;                 // field A output (interior cells)
     float *pre;                // pre-blend values of pad cells
@@ -137,92 +145,103 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
 // coefficient-major table; with fixed coefficients the table has one column
 // and the values are loaded once per warp into registers (cc).
 template <int MMAX, bool ADAPT>
-__device__ __forceinline__ const float *coef_base(const StepArgs &a, float vc)
+__device__ __forceinline__ void load_coefs(const StepArgs &a, float vc, const float *cc, float *cf)
 {
-    int bin = 0;
-    if (ADAPT) {
-        bin = (int)((vc - a.vmin) / a.dv + 0.5f);
-        bin = min(max(bin, 0), a.nbins - 1);
+    if (!ADAPT) {
+#pragma unroll
+        for (int l = 0; l <= MMAX; ++l) cf[l] = cc[l];
+        return;
     }
-    return a.ctab + bin;
+    int bin = (int)((vc - a.vmin) / a.dv + 0.5f);
+    bin = min(max(bin, 0), a.nbins - 1);
+    constexpr int Q = (MMAX + 4) / 4;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float4 g = __ldg(a.ctab4 + (long)q * a.nbins + bin);
+        if (4 * q + 0 <= MMAX) cf[4 * q + 0] = g.x;
+        if (4 * q + 1 <= MMAX) cf[4 * q + 1] = g.y;
+        if (4 * q + 2 <= MMAX) cf[4 * q + 2] = g.z;
+        if (4 * q + 3 <= MMAX) cf[4 * q + 3] = g.w;
+    }
 }
 
 // Spatial operator of one cell: w = k0*c0*u + sum_l c_l*((u[z-l]+u[z+l])*hzx2_1
 // + u[x-l] + u[x+l]) (kernel.cu:59-72), with q the column's register queue
 // (centre at index C) and row the cell's row in the staged halo box.
 template <int MMAX, bool ADAPT>
-__device__ __forceinline__ float lap_cell(const float *q, int C, const float *row, const float *cb,
-                                          const float *cc, int nbins, float k0, float hzx2_1)
+__device__ __forceinline__ float lap_cell(const float *q, int C, const float *row, const float *cf,
+                                          float k0, float hzx2_1)
 {
-    float w1 = k0 * (ADAPT ? __ldg(cb) : cc[0]) * q[C];
+    float w1 = k0 * cf[0] * q[C];
 #pragma unroll
     for (int l = 1; l <= MMAX; ++l) {
         const float xs = (q[C - l] + q[C + l]) * hzx2_1 + row[-l];
-        w1 = fmaf(ADAPT ? __ldg(cb + l * nbins) : cc[l], xs + row[l], w1);
+        w1 = fmaf(cf[l], xs + row[l], w1);
     }
     return w1;
 }
 
-// One time step of a batch of shots on one 128 x 16 tile (grid: tiles x
-// tiles x shots).  All inputs arrive by TMA into shared memory under one
-// mbarrier; the warp's lanes each own one column and stream its rows through
-// register queues; outputs are stored directly.
-template <int MMAX, bool ADAPT, int MODE>
-__global__ void __launch_bounds__(NTHREADS)
-    k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
-           const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
-           const __grid_constant__ CUtensorMap flatV, const __grid_constant__ ImgMaps img,
-           const StepArgs a)
+// Shared-memory pointers of one pipeline stage (one tile's staged inputs).
+template <int MMAX, int MODE>
+struct Stage {
+    float *tA, *tS, *fA0, *fV, *fS0, *fR1, *fR2, *fSa, *fRa;
+    __device__ __forceinline__ explicit Stage(float *base)
+    {
+        using S = Shape<MMAX>;
+        tA = base;
+        tS = base + S::ELEMS;  // backward only
+        float *fl = base + Smem<MMAX, MODE>::NBOX * S::ELEMS;
+        fA0 = fl; fV = fl + FLAT;
+        fS0 = fl + 2 * FLAT; fR1 = fl + 3 * FLAT; fR2 = fl + 4 * FLAT;
+        fSa = fl + 5 * FLAT; fRa = fl + 6 * FLAT;
+    }
+};
+
+// Stage bytes without the barrier word(s).
+template <int MMAX, int MODE>
+__host__ __device__ constexpr unsigned stage_bytes() { return Smem<MMAX, MODE>::BYTES - 16u; }
+
+// TMA loads of one tile's inputs into a stage, completing on `bar`
+// (issued by one thread).
+template <int MMAX, int MODE>
+__device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t *bar,
+                                           const CUtensorMap &mapA, const CUtensorMap &mapS,
+                                           const CUtensorMap &flatA0, const CUtensorMap &flatS0,
+                                           const CUtensorMap &flatV, const ImgMaps &img, int x0,
+                                           int z0, int shot, int vshot)
 {
     using S = Shape<MMAX>;
-    using SM = Smem<MMAX, MODE>;
+    mbar_arrive_expect_tx(bar, stage_bytes<MMAX, MODE>());
+    tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
+    tma_load_3d(st.fA0, &flatA0, x0, z0, shot, bar);
+    tma_load_3d(st.fV, &flatV, x0, z0, vshot ? shot : 0, bar);
+    if (MODE == MODE_BWD) {
+        tma_load_3d(st.tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, bar);
+        tma_load_3d(st.fS0, &flatS0, x0, z0, shot, bar);
+        tma_load_3d(st.fR1, &img.rel1, x0, z0, shot, bar);
+        tma_load_3d(st.fR2, &img.rel2, x0, z0, shot, bar);
+        tma_load_3d(st.fSa, &img.sacc, x0, z0, shot, bar);
+        tma_load_3d(st.fRa, &img.racc, x0, z0, shot, bar);
+    }
+}
+
+// The update of one staged 128 x 16 tile (after its copies landed and the
+// out-of-grid halo was mirrored): the warp's lanes each own one column and
+// stream its rows through register queues; outputs are stored directly.
+// Coefficients are gathered PF rows ahead of their use (adaptive mode): a
+// gather depends on the staged velocity and usually misses L1, so issuing it
+// early hides its latency behind the rows in between.
+template <int MMAX, bool ADAPT, int MODE, int PF>
+__device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX, MODE> &st,
+                                             const float *cc, int x0, int z0, int shot, int NX)
+{
+    using S = Shape<MMAX>;
     constexpr int QN = 2 * MMAX + 1;
-    extern __shared__ __align__(128) float smem[];
-    float *tA = smem;
-    float *tS = smem + S::ELEMS;                          // backward only
-    float *fl = smem + SM::NBOX * S::ELEMS;               // flat tiles
-    float *fA0 = fl, *fV = fl + FLAT;
-    float *fS0 = fl + 2 * FLAT, *fR1 = fl + 3 * FLAT, *fR2 = fl + 4 * FLAT;
-    float *fSa = fl + 5 * FLAT, *fRa = fl + 6 * FLAT;
-    uint64_t &bar = *reinterpret_cast<uint64_t *>(fl + SM::NFLAT * FLAT);
+    const float *tA = st.tA, *tS = st.tS, *fA0 = st.fA0, *fV = st.fV, *fS0 = st.fS0;
+    const float *fR1 = st.fR1, *fR2 = st.fR2, *fSa = st.fSa, *fRa = st.fRa;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wx = warp % WX, wz = warp / WX;
-    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z;
-    const int NX = a.nxs[shot];
-    if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
-
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(&bar, SM::BYTES - 16u);
-        tma_load_3d(tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, &bar);
-        tma_load_3d(fA0, &flatA0, x0, z0, shot, &bar);
-        tma_load_3d(fV, &flatV, x0, z0, a.vshot ? shot : 0, &bar);
-        if (MODE == MODE_BWD) {
-            tma_load_3d(tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, &bar);
-            tma_load_3d(fS0, &flatS0, x0, z0, shot, &bar);
-            tma_load_3d(fR1, &img.rel1, x0, z0, shot, &bar);
-            tma_load_3d(fR2, &img.rel2, x0, z0, shot, &bar);
-            tma_load_3d(fSa, &img.sacc, x0, z0, shot, &bar);
-            tma_load_3d(fRa, &img.racc, x0, z0, shot, &bar);
-        }
-    }
-    // fixed coefficients: once per thread, while the copies are in flight
-    float cc[MMAX + 1];
-#pragma unroll
-    for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
     const int src = a.src[shot];
-    if (!mbar_wait_bounded(&bar, 0, &g_rtm_dev_error)) {
-        mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
-        return;
-    }
-    patch_halo<MMAX>(tA, x0, z0, NX, a.NZ);
-    if (MODE == MODE_BWD) patch_halo<MMAX>(tS, x0, z0, NX, a.NZ);
-    __syncthreads();
-
     const long long so = (long long)shot * a.ss;
     const int zw = z0 + wz * RW;             // first row of this warp
     const int gx = x0 + wx * 32 + lane;      // this lane's column
@@ -236,6 +255,13 @@ __global__ void __launch_bounds__(NTHREADS)
     const bool col_ok = gx < NX;
     const long long g0 = so + (long)zw * a.P + gx;  // global index of row zw
 
+    // Coefficients are gathered PF rows ahead of their use (adaptive mode):
+    // a gather depends on the staged velocity and usually misses L1, so
+    // issuing it early hides its latency behind the rows in between.
+    float cfr[RW][MMAX + 1];
+#pragma unroll
+    for (int i = 0; i < PF; ++i) load_coefs<MMAX, ADAPT>(a, fV[fr + i * TX], cc, cfr[i]);
+
     if (MODE == MODE_FWD) {
         // two rows per iteration: two independent accumulation chains
         float q[QN + 1];
@@ -243,6 +269,10 @@ __global__ void __launch_bounds__(NTHREADS)
         for (int j = 0; j < QN - 1; ++j) q[j] = tA[(rbase + j) * S::BW + cx];
 #pragma unroll
         for (int i = 0; i < RW; i += 2) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (i + h + PF < RW)
+                    load_coefs<MMAX, ADAPT>(a, fV[fr + (i + h + PF) * TX], cc, cfr[i + h + PF]);
             q[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
             q[QN] = tA[(rbase + i + QN) * S::BW + cx];
 #pragma unroll
@@ -251,14 +281,17 @@ __global__ void __launch_bounds__(NTHREADS)
                 if (z >= NZ) continue;
                 const int t = fr + (i + h) * TX;
                 const float vc = fV[t];
-                const float *cb = coef_base<MMAX, ADAPT>(a, vc);
+                const float *cf = cfr[i + h];
                 const float *row = tA + (rbase + i + h + MMAX) * S::BW + cx;
-                const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cb, cc, a.nbins, a.k0, a.hzx2_1);
+                const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cf, a.k0, a.hzx2_1);
                 float val = fmaf(vc * vc * a.tao2 * a.h2, w1, 2.0f * q[MMAX + h] - fA0[t]);
                 if (z == src_z && gx == src_x) val += a.wavelet;
                 if (col_ok) {
                     const bool interior = col_in && z >= N2 && z < NZ - N2;
-                    (interior ? a.a2 : a.pre)[g0 + (long)(i + h) * a.P] = val;
+                    const long long g = g0 + (long)(i + h) * a.P;
+                    if (interior) a.a2[g] = val;
+                    if (!interior || gx == N2 || gx == NX - 1 - N2 || z == N2 || z == NZ - 1 - N2)
+                        a.pre[g] = val;
                 }
             }
 #pragma unroll
@@ -285,6 +318,7 @@ __global__ void __launch_bounds__(NTHREADS)
     }
 #pragma unroll
     for (int i = 0; i < RW; ++i) {
+        if (i + PF < RW) load_coefs<MMAX, ADAPT>(a, fV[fr + (i + PF) * TX], cc, cfr[i + PF]);
         qr[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
         if (rows_s) qs[QN - 1] = tS[(rbase + i + QN - 1) * S::BW + cx];
         const int z = zw + i;
@@ -292,15 +326,15 @@ __global__ void __launch_bounds__(NTHREADS)
             const int t = fr + i * TX;
             const float vc = fV[t];
             const float vv = vc * vc * a.tao2 * a.h2;
-            const float *cb = coef_base<MMAX, ADAPT>(a, vc);
+            const float *cf = cfr[i];
             const float *rowR = tA + (rbase + i + MMAX) * S::BW + cx;
             const float *rowS = tS + (rbase + i + MMAX) * S::BW + cx;
-            const float c0 = ADAPT ? __ldg(cb) : cc[0];
+            const float c0 = cf[0];
             float wr = a.k0 * c0 * qr[MMAX];
             float ws = a.k0 * c0 * qs[MMAX];
 #pragma unroll
             for (int l = 1; l <= MMAX; ++l) {
-                const float cl = ADAPT ? __ldg(cb + l * a.nbins) : cc[l];
+                const float cl = cf[l];
                 wr = fmaf(cl, (qr[MMAX - l] + qr[MMAX + l]) * a.hzx2_1 + rowR[-l] + rowR[l], wr);
                 if (rows_s)
                     ws = fmaf(cl, (qs[MMAX - l] + qs[MMAX + l]) * a.hzx2_1 + rowS[-l] + rowS[l], ws);
@@ -323,7 +357,11 @@ __global__ void __launch_bounds__(NTHREADS)
             }
             const bool interior = col_in && z >= N2 && z < NZ - N2;
             const long long g = g0 + (long)i * a.P;
-            if (col_ok) (interior ? a.a2 : a.pre)[g] = rv;
+            if (col_ok) {
+                if (interior) a.a2[g] = rv;
+                if (!interior || gx == N2 || gx == NX - 1 - N2 || z == N2 || z == NZ - 1 - N2)
+                    a.pre[g] = rv;
+            }
             if (interior) {
                 float sv = fmaf(vv, ws, 2.0f * qs[MMAX] - fS0[t]);
                 if (z == src_z && gx == src_x) sv += a.wavelet;
@@ -349,17 +387,155 @@ __global__ void __launch_bounds__(NTHREADS)
     }
 }
 
+#ifndef RTM_FWD_MINB
+#define RTM_FWD_MINB 4
+#endif
+#ifndef RTM_FWD_PF
+#define RTM_FWD_PF 0
+#endif
+#ifndef RTM_PIPE_FWD_PF
+#define RTM_PIPE_FWD_PF 2
+#endif
+
+// One time step of a batch of shots, one CTA per 128 x 16 tile (grid: tiles
+// x tiles x shots).  All inputs arrive by TMA into shared memory under one
+// mbarrier.
+template <int MMAX, bool ADAPT, int MODE>
+__global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : RTM_FWD_MINB)
+    k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
+           const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
+           const __grid_constant__ CUtensorMap flatV, const __grid_constant__ ImgMaps img,
+           const StepArgs a)
+{
+    using SM = Smem<MMAX, MODE>;
+    constexpr int PF = MODE == MODE_FWD ? RTM_FWD_PF : (MMAX <= 8 ? 4 : 2);  // register budget
+    extern __shared__ __align__(128) float smem[];
+    const Stage<MMAX, MODE> st(smem);
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z;
+    const int NX = a.nxs[shot];
+    if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) issue_tile<MMAX, MODE>(st, &bar, mapA, mapS, flatA0, flatS0, flatV, img, x0, z0, shot, a.vshot);
+    // fixed coefficients: once per thread, while the copies are in flight
+    float cc[MMAX + 1];
+#pragma unroll
+    for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
+    const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
+    if (ok) {
+        patch_halo<MMAX>(st.tA, x0, z0, NX, a.NZ);
+        if (MODE == MODE_BWD) patch_halo<MMAX>(st.tS, x0, z0, NX, a.NZ);
+    }
+    if (!__syncthreads_and(ok)) {
+        mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
+        return;
+    }
+    compute_tile<MMAX, ADAPT, MODE, PF>(a, st, cc, x0, z0, shot, NX);
+}
+
+// Persistent form of k_step: a fixed grid of CTAs walks the batch's tiles
+// (item i -> shot, tile row, tile column; shots may differ in width) with a
+// two-stage TMA pipeline, loading tile k+1 while tile k is computed.
+// items[s] = first item of shot s (items[nb] = total).
+template <int MMAX, int MODE>
+struct PipeSmem {
+    static constexpr unsigned BYTES = 2 * stage_bytes<MMAX, MODE>() + 16u;
+};
+
+__device__ __forceinline__ void decode_item(const int *items, int nb, const int *nxs, int NZ, int it,
+                                            int &shot, int &x0, int &z0)
+{
+    int lo = 0, hi = nb - 1;  // last shot whose first item is <= it
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(items + mid) <= it) lo = mid; else hi = mid - 1;
+    }
+    shot = lo;
+    const int ntx = (__ldg(nxs + shot) + TX - 1) / TX;
+    const int r = it - __ldg(items + shot);
+    z0 = (r / ntx) * TZ;
+    x0 = (r % ntx) * TX;
+}
+
+template <int MMAX, bool ADAPT, int MODE>
+__global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
+    k_step_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
+                const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
+                const __grid_constant__ CUtensorMap flatV, const __grid_constant__ ImgMaps img,
+                const StepArgs a, const int *__restrict__ items, int nb)
+{
+    constexpr int PF = MODE == MODE_BWD ? RW : RTM_PIPE_FWD_PF;
+    constexpr unsigned SB = stage_bytes<MMAX, MODE>();
+    extern __shared__ __align__(128) float smem[];
+    const Stage<MMAX, MODE> st0(smem), st1(reinterpret_cast<float *>(reinterpret_cast<char *>(smem) + SB));
+    uint64_t *bar = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + 2 * SB);
+    const int total = __ldg(items + nb);
+    int it = blockIdx.x;
+    if (it >= total) return;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    int shot, x0, z0;
+    decode_item(items, nb, a.nxs, a.NZ, it, shot, x0, z0);
+    if (threadIdx.x == 0)
+        issue_tile<MMAX, MODE>(st0, bar, mapA, mapS, flatA0, flatS0, flatV, img, x0, z0, shot, a.vshot);
+    float cc[MMAX + 1];
+#pragma unroll
+    for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
+    unsigned phase = 0;  // bit s: parity of stage s's next completion
+    for (int k = 0; it < total; ++k, it += gridDim.x) {
+        const int s = k & 1;
+        const Stage<MMAX, MODE> &cur = s ? st1 : st0;
+        const int nit = it + gridDim.x;
+        int nshot = 0, nx0 = 0, nz0 = 0;
+        if (nit < total) {
+            decode_item(items, nb, a.nxs, a.NZ, nit, nshot, nx0, nz0);
+            if (threadIdx.x == 0) {
+                // the other stage was last read (and patched) in the previous
+                // iteration, which ended with a block barrier
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_tile<MMAX, MODE>(s ? st0 : st1, bar + (s ^ 1), mapA, mapS, flatA0, flatS0, flatV,
+                                       img, nx0, nz0, nshot, a.vshot);
+            }
+        }
+        const int NX = __ldg(a.nxs + shot);
+        const bool ok = mbar_wait_bounded(bar + s, (phase >> s) & 1u, &g_rtm_dev_error);
+        if (ok) {
+            patch_halo<MMAX>(cur.tA, x0, z0, NX, a.NZ);
+            if (MODE == MODE_BWD) patch_halo<MMAX>(cur.tS, x0, z0, NX, a.NZ);
+        }
+        if (!__syncthreads_and(ok)) {
+            // let the copies in flight land before the CTA exits
+            mbar_wait_bounded(bar + s, (phase >> s) & 1u, &g_rtm_dev_error);
+            if (nit < total) mbar_wait_bounded(bar + (s ^ 1), (phase >> (s ^ 1)) & 1u, &g_rtm_dev_error);
+            return;
+        }
+        phase ^= 1u << s;
+        compute_tile<MMAX, ADAPT, MODE, PF>(a, cur, cc, x0, z0, shot, NX);
+        __syncthreads();  // every thread is done with this stage before it is reloaded
+        shot = nshot; x0 = nx0; z0 = nz0;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Pad kernel: one-way update + blend of the absorbing pad (kernel.cu:116-183),
 // ring save / restore, receiver recording.
 
 struct PadArgs {
-    int NZ, P, N2;
+    int NZ, P, N2, M;
     long long ss;
     long nabc;                // pad cells of the widest grid (threads per shot)
     const int *nxs, *rx0s;    // per-shot padded width and receiver start column
     long long tab_ss;         // pad-table entries between shots (0: shared table)
-    const int4 *meta;         // [nabc] {z, x, kind | dz<<2 | dx<<4, ring slot index or -1}
+    const int4 *meta;         // [nabc] pad_meta(): {cell, d1, d2, (ring slot + 1) << 1 | corner}
     const float4 *fac;        // [nabc] side: {taoh*v, 1/(taoh*v+1), taoh2*vq*vq, w}
                               //        corner: {r_1, 1/(2 r_1+1), 0, w}
     const float *a0, *a1;     // field A levels k-2, k-1
@@ -422,6 +598,30 @@ __host__ __device__ __forceinline__ long ring_index(int z, int x, int NZ, int NX
     return -1;
 }
 
+// Geometry of pad cell t as flat offsets in a grid of pitch P:
+// {cell, d1, d2, (ring slot + 1) << 1 | corner}.  Row-edge cell: inward
+// neighbour cell+d1 (d1 = dz*P), lateral step d2 = 1; column-edge cell:
+// d1 = dx, d2 = P; corner: its two inward neighbours cell+d1 (d1 = dx) and
+// cell+d2 (d2 = dz*P).  dz / dx point into the grid.  Ring slot -1 (stored as
+// 0) when the cell is not on the saved ring.
+__host__ __device__ __forceinline__ int4 pad_meta(long t, int NZ, int NX, int P, int N2, int M)
+{
+    const AbcCell cc = abc_cell(t, NZ, NX, N2);
+    const int z = cc.z, x = cc.x;
+    const int ea = min(z, NZ - 1 - z), ee = min(x, NX - 1 - x);
+    const int dz = (z < NZ - 1 - z) ? 1 : -1, dx = (x < NX - 1 - x) ? 1 : -1;
+    const long ri = M > 0 ? ring_index(z, x, NZ, NX, N2, M, NZ - 2 * N2, NX - 2 * N2) : -1;
+    int d1, d2, corner = 0;
+    if (ee >= ea + 2) {
+        d1 = dz * P; d2 = 1;
+    } else if (ea >= ee + 2) {
+        d1 = dx; d2 = P;
+    } else {
+        d1 = dx; d2 = dz * P; corner = 1;
+    }
+    return make_int4(z * P + x, d1, d2, (int)((ri + 1) << 1) | corner);
+}
+
 // One-way update + blend of one pad cell (kernel.cu:116-183).  Side cell c
 // with inward neighbour n and lateral step s:
 //   b = inv*(A*(u2[n]-u0[n]+u0[c]) - (-2u1[c]+u0[c]+u2[n]-2u1[n]+u0[n])
@@ -453,49 +653,47 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         return;
     }
     if (t >= abc_count(a.NZ, NX, a.N2)) return;  // this shot's pad is smaller
+    // Neighbour values of level k before blending come from `pre`, which the
+    // stencil kernel fills for every pad cell and the first interior ring.
     const int4 m = __ldg(a.meta + shot * a.tab_ss + t);
     const float4 f = __ldg(a.fac + shot * a.tab_ss + t);
-    const int z = m.x, x = m.y, kind = m.z & 3;
-    const int dz = ((m.z >> 2) & 3) == 1 ? 1 : -1, dx = ((m.z >> 4) & 3) == 1 ? 1 : -1;
-    const int NZ = a.NZ, N2 = a.N2, P = a.P;
-    const long c = (long)z * P + x;
-    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so, *in2 = a.a2 + so;
-    auto pv = [&](int zz, int xx) -> float {
-        const long i = (long)zz * P + xx;
-        return is_pad(zz, xx, NZ, NX, N2) ? pr[i] : in2[i];
-    };
+    const long c = m.x;
+    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so;
     float b;
-    if (kind != PAD_CORNER) {
-        int nz_, nx_, sz, sx;
-        if (kind == PAD_ROWEDGE) {
-            nz_ = z + dz; nx_ = x; sz = 0; sx = 1;
-        } else {
-            nz_ = z; nx_ = x + dx; sz = 1; sx = 0;
-        }
-        const long n = (long)nz_ * P + nx_;
-        const float u2n = pv(nz_, nx_);
-        const float lat = pv(nz_ + sz, nx_ + sx) - 2.0f * u2n + pv(nz_ - sz, nx_ - sx) +
-                          u0[(long)(z + sz) * P + x + sx] - 2.0f * u0[c] + u0[(long)(z - sz) * P + x - sx];
-        b = f.y * (f.x * (u2n - u0[n] + u0[c]) - (-2.0f * u1[c] + u0[c] + u2n - 2.0f * u1[n] + u0[n]) +
+    if (!(m.w & 1)) {
+        const long n = c + m.y, sd = m.z;
+        const float u2n = pr[n];
+        const float u0c = u0[c], u0n = u0[n];
+        const float lat = pr[n + sd] - 2.0f * u2n + pr[n - sd] + u0[c + sd] - 2.0f * u0c + u0[c - sd];
+        b = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1[c] + u0c + u2n - 2.0f * u1[n] + u0n) +
                    f.z * lat);
     } else {
-        b = f.y * (u1[c] + f.x * (pv(z, x + dx) + pv(z + dz, x)));
+        b = f.y * (u1[c] + f.x * (pr[c + m.y] + pr[c + m.z]));
     }
     const float out = (1.0f - f.w) * pr[c] + f.w * b;
     a.a2[so + c] = out;
-    if (a.ring_mode && m.w >= 0) {
+    const long ri = a.ring_mode ? (long)(m.w >> 1) - 1 : -1;
+    if (ri >= 0) {
         if (a.ring_prec == 0) {
             if (a.ring_mode == 1)
-                a.ring[(long long)shot * a.ring_ss + m.w] = out;
+                a.ring[(long long)shot * a.ring_ss + ri] = out;
             else
-                a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + m.w];
+                a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + ri];
         } else if (a.ring_mode == 1) {
-            a.stage[(long long)shot * a.ringsz + m.w] = out;
-            atomicMax(a.amax + (long long)shot * a.slots + a.slot, __float_as_uint(fabsf(out)));
+            a.stage[(long long)shot * a.ringsz + ri] = out;
         } else {
             const long long sl = (long long)shot * a.slots + a.slot;
-            a.s2[so + c] = ring_dequant(a.ring16[sl * a.ringsz + m.w], a.scale[sl], a.ring_prec);
+            a.s2[so + c] = ring_dequant(a.ring16[sl * a.ringsz + ri], a.scale[sl], a.ring_prec);
         }
+    }
+    if (a.ring_prec && a.ring_mode == 1) {
+        // max |value| of the step's ring: reduced over the warp first (all
+        // lanes of a block belong to one shot), one atomic per warp.  Float
+        // bits of non-negative values order like unsigned integers.
+        const unsigned mask = __activemask();
+        const unsigned bits = __reduce_max_sync(mask, ri >= 0 ? __float_as_uint(fabsf(out)) : 0u);
+        if ((threadIdx.x & 31) == __ffs(mask) - 1 && bits)
+            atomicMax(a.amax + (long long)shot * a.slots + a.slot, bits);
     }
 }
 
@@ -636,8 +834,7 @@ __global__ void k_pad_tables(const float *vs, const float *r1s, const float *w, 
         const float tv = __fmul_rn(taoh, vc);
         f = make_float4(tv, __fdiv_rn(1.0f, __fadd_rn(tv, 1.0f)), __fmul_rn(__fmul_rn(taoh2, vq), vq), wj);
     }
-    const long ri = M > 0 ? ring_index(z, x, NZ, NX, N2, M, NZ - 2 * N2, NX - 2 * N2) : -1;
-    meta[shot * tab_ss + t] = make_int4(z, x, kind | ((dz > 0 ? 1 : 2) << 2) | ((dx > 0 ? 1 : 2) << 4), (int)ri);
+    meta[shot * tab_ss + t] = pad_meta(t, NZ, NX, P, N2, M);
     fac[shot * tab_ss + t] = f;
 }
 

@@ -60,6 +60,31 @@ class Engine:
         capi.check(capi.lib().rtm_ctx_bytes(self._h, C.byref(n)), "ctx_bytes")
         return int(n.value)
 
+    def set_kernel(self, fwd: int, bwd: int | None = None, shots_per_launch: int = 0):
+        """Stencil kernel form per phase (capi.RTM_KERNEL_TILED / _PERSISTENT)
+        and shots per launch (0: the context's batch)."""
+        bwd = fwd if bwd is None else bwd
+        capi.check(capi.lib().rtm_ctx_set_kernel(self._h, fwd, bwd, shots_per_launch), "set_kernel")
+
+    def kernel(self):
+        f, b, n = C.c_int(), C.c_int(), C.c_int()
+        capi.check(capi.lib().rtm_ctx_get_kernel(self._h, C.byref(f), C.byref(b), C.byref(n)),
+                   "get_kernel")
+        return {"fwd": f.value, "bwd": b.value, "shots_per_launch": n.value}
+
+    def autotune(self, src_cells, win_x0=None, win_nx=None, nsteps: int = 20) -> float:
+        """Times the kernel forms and shots per launch on the first shots of
+        a survey, keeps the fastest; returns its Gcell-updates/s."""
+        src = self._src(src_cells)
+        x0 = None if win_x0 is None else np.ascontiguousarray(win_x0, np.int32)
+        wn = None if win_nx is None else np.ascontiguousarray(win_nx, np.int32)
+        rate = C.c_double()
+        capi.check(capi.lib().rtm_ctx_autotune(self._h, len(src), capi.iptr(src),
+                                               None if x0 is None else capi.iptr(x0),
+                                               None if wn is None else capi.iptr(wn), nsteps,
+                                               C.byref(rate)), "autotune")
+        return rate.value
+
     def set_timing(self, on: bool):
         capi.check(capi.lib().rtm_ctx_set_timing(self._h, int(on)), "set_timing")
 
@@ -154,3 +179,16 @@ class Engine:
                                                         int(nrec_div), int(inorm), ip_, lp, flags),
                    "migrate_stack_windows")
         return image, illum
+
+
+def plain_migrate_shot(prob: Problem, src_cell: int, seis):
+    """The reference's per-shot launch sequence on the drop-in kernels
+    (rtm_plain_migrate_shot): full padded rel1, rel2 [NZ, NX]."""
+    p = prob.c_struct()
+    seis = np.ascontiguousarray(seis, np.float32)
+    rel1 = np.zeros((prob.NZ, prob.NX), np.float32)
+    rel2 = np.zeros_like(rel1)
+    capi.check(capi.lib().rtm_plain_migrate_shot(C.byref(p), int(src_cell), capi.fptr(seis),
+                                                 capi.fptr(rel1), capi.fptr(rel2)),
+               "plain_migrate_shot")
+    return rel1, rel2

@@ -150,3 +150,17 @@ def run_reference_loop(L, p, seis):
         else:
             ok(L.rtm_k_Rel_NonCompen(vp(FW2), vp(BW2), vp(R1), vp(R2), NZ, NX, None))
     return host(R1), host(R2)
+
+
+def test_plain_shot_driver(product_lib, cuda_ok):
+    """rtm_plain_migrate_shot (the reference's loop in C++ on the drop-in
+    kernels) against the oracle."""
+    from rtm_gpu_gb300.engine import plain_migrate_shot
+    for adaptive, compen in ((True, True), (False, False)):
+        p = small_problem(adaptive=adaptive, compen=compen, NT=120)
+        rng = np.random.default_rng(8)
+        seis = (rng.standard_normal((p.nrec, p.NT)) * 1e-2).astype(np.float32)
+        o1, o2 = orc.migrate(p, seis)
+        g1, g2 = plain_migrate_shot(p, p.src_flat(), seis)
+        assert rel_l2(interior(p, g1), interior(p, o1)) < 1e-4
+        assert rel_l2(interior(p, g2), interior(p, o2)) < 1e-4
