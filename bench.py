@@ -164,6 +164,18 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def measured_traffic(cfg, shots_per_launch):
+    """DRAM bytes of one backward-stencil launch from the committed ncu
+    capture of this workload (profiles/ncu_traffic.json), or None."""
+    key = "k_step backward, %s M=%d, %dx%d, %d shots per launch" % (
+        cfg.coef, cfg.M, cfg.nz, cfg.nx, shots_per_launch)
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))[key]
+        return {"bytes": d["dram_bytes_read"] + d["dram_bytes_write"], "source": "profiles/" + d["summary"]}
+    except Exception:
+        return None
+
+
 def cpu_baseline(cfg, pmig, shots, seis_host, nt_sample, threads):
     """Reference kernel bodies (oracle/_ref) or, failing that, the oracle's
     C restatement, timed on the host cores on one shot with nt_sample steps."""
@@ -455,9 +467,11 @@ def main():
     bwd_ms = tm["bwd_ms"] / max(tm["bwd_n"], 1)
     fwd_ms = tm["fwd_ms"] / max(tm["fwd_n"], 1)
     peak, peak_kind = measured_peak()
+    traffic = measured_traffic(cfg, nb)
     achieved = bwd_bytes / (bwd_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak, "traffic": (traffic or {}).get("bytes"),
+                "traffic_source": (traffic or {}).get("source"),
                 "kernel": "k_step<backward> (source reconstruction + receiver step + imaging)",
                 "bytes_per_launch": bwd_bytes, "launch_ms": bwd_ms, "peak_kind": peak_kind,
                 "forward_kernel": {"launch_ms": fwd_ms, "bytes_per_launch": fwd_bytes,

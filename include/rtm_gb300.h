@@ -38,7 +38,8 @@ enum {
     RTM_ERR_CUDA = -2,      /* CUDA runtime error (message in rtm_last_error)   */
     RTM_ERR_NOMEM = -3,     /* device or host allocation failed                 */
     RTM_ERR_DEVICE = -4,    /* a kernel reported a device-side error            */
-    RTM_ERR_UNSUPPORTED = -5
+    RTM_ERR_UNSUPPORTED = -5,
+    RTM_ERR_IO = -6         /* a file could not be read or written              */
 };
 
 const char *rtm_last_error(void);
@@ -307,6 +308,29 @@ int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
  * afterwards. */
 int rtm_ctx_autotune(rtm_ctx *ctx, int nshot, const int *src_cells, const int *win_x0,
                      const int *win_nx, int nsteps, double *gcells_per_s);
+
+/* ======================================================================
+ * 5. The reference's file flow.
+ * ====================================================================== */
+
+/* Resample.cpp:193-225 (resample, called per trace at kernel.cu:839-845):
+ * ntrace traces yin[ntrace][nxin] at interval dxin to yout[ntrace][nxout] at
+ * dxout by the 8-point least-squares sinc interpolator; bit-identical to the
+ * reference.  flags: RTM_DEVICE_PTRS for device buffers. */
+int rtm_resample(const float *yin, int ntrace, int nxin, float dxin, float *yout, int nxout,
+                 float dxout, int flags);
+
+/* kernel.cu:542-1098 up to the stacked image: reads the reference's run file
+ * (the 2D_Real_RVSP_RTM.txt layout: 28 label/value pairs), the parameter,
+ * source-depth, velocity and per-shot gather files it names (paths relative
+ * to the working directory, as the reference opens them), resamples the
+ * gathers when their interval differs from the modelling step, migrates all
+ * shots on the batched engine (max_batch shots per launch, 0: 16) and writes
+ * RVSP_RTM_up_<m>.dat / RVSP_RTM_down_<m>.dat per shot,
+ * RVSP_Migration_Real_new2.dat and vnew.dat with the reference's names and
+ * layouts.  The post-stack display chain that follows in the reference
+ * (depth/time conversion, phase rotation, SEG-Y) is not part of this call. */
+int rtm_run_config(const char *run_file, int max_batch);
 
 #ifdef __cplusplus
 }

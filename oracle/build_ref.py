@@ -10,9 +10,9 @@ TEST INFRASTRUCTURE ONLY.  Products:
   verbatim from a reference checkout into ``oracle/_ref/`` (git-ignored; the
   repository never holds reference source).  Once copied, the fragments let
   the library be rebuilt on a machine without the checkout.
-* ``oracle/_ref/libref_host.so`` -- LSMOrCon_rec_2D.cpp and
-  GPU_velocity_real.cpp compiled in place from the checkout (only where the
-  checkout exists; used to generate the golden fixtures).
+* ``oracle/_ref/libref_host.so`` -- LSMOrCon_rec_2D.cpp,
+  GPU_velocity_real.cpp and Resample.cpp compiled in place from the checkout
+  (only where the checkout exists; used to generate the golden fixtures).
 
 Everything is compiled with ``-ffp-contract=off`` so that neither x86-64 nor
 aarch64 fuses multiply-adds: the FP32 oracle then reproduces the reference's
@@ -49,9 +49,10 @@ def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     out = os.path.join(BUILD, "liboracle.so")
     srcs = [os.path.join(HERE, f) for f in
-            ("rtm_oracle.c", "lsm_oracle.c", "rtm_oracle_body.h", "rtm_driver_body.h", "rtm_oracle.h")]
+            ("rtm_oracle.c", "lsm_oracle.c", "resample_oracle.c", "rtm_oracle_body.h",
+             "rtm_driver_body.h", "rtm_oracle.h")]
     if force or _stale(out, srcs):
-        _run(["gcc", *CFLAGS, "-std=gnu11", "-o", out + ".tmp", srcs[0], srcs[1], "-lm"])
+        _run(["gcc", *CFLAGS, "-std=gnu11", "-o", out + ".tmp", srcs[0], srcs[1], srcs[2], "-lm"])
         os.replace(out + ".tmp", out)
     return out
 
@@ -93,7 +94,8 @@ def build_ref(checkout: str = DEFAULT_CHECKOUT, force: bool = False) -> dict:
         out = os.path.join(REF_OUT, "libref_host.so")
         srcs = [os.path.join(HERE, "ref_host_shim.cpp"),
                 os.path.join(checkout, "LSMOrCon_rec_2D.cpp"),
-                os.path.join(checkout, "GPU_velocity_real.cpp")]
+                os.path.join(checkout, "GPU_velocity_real.cpp"),
+                os.path.join(checkout, "Resample.cpp")]
         if force or _stale(out, srcs):
             _run(["g++", *CFLAGS, "-w", "-I", checkout, "-o", out + ".tmp", srcs[0]])
             os.replace(out + ".tmp", out)

@@ -73,6 +73,8 @@ def lib():
                                      C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                      _i32p, _i32p, _i32p, C.c_void_p, C.c_int, C.c_double]
         L.ls_taylor.argtypes = [C.c_int, _f32p]
+        L.or_resample.argtypes = [C.c_int, C.c_float, _f32p, C.c_int, C.c_float, _f32p]
+        L.rs_table.argtypes = [_f32p]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_threads.restype = C.c_int
         _lib = L
@@ -122,6 +124,7 @@ def ref_host():
                                    C.c_double, _i32p, _i32p, _i32p, _f32p, C.c_int, C.c_double]
         L.ref_velocity.argtypes = [C.c_char_p, _f32p, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int,
                                    C.c_int, C.c_float, C.c_float, C.c_int]
+        L.ref_resample.argtypes = [C.c_int, C.c_float, _f32p, C.c_int, C.c_float, _f32p]
         _refh = L
     return _refh
 
@@ -277,6 +280,23 @@ def ls_coefs(r, bb, M, hzx=1.0):
     c = np.zeros(M + 1, np.float64)
     lib().ls_coefs(c, r, bb, M, hzx)
     return c
+
+
+def resample(y, dxin, nxout, dxout):
+    """Trace(s) y[..., nxin] resampled to nxout samples at dxout
+    (Resample.cpp:193-225)."""
+    y = np.ascontiguousarray(y, np.float32)
+    flat = y.reshape(-1, y.shape[-1])
+    out = np.zeros((flat.shape[0], nxout), np.float32)
+    for i in range(flat.shape[0]):
+        lib().or_resample(flat.shape[1], dxin, np.ascontiguousarray(flat[i]), nxout, dxout, out[i])
+    return out.reshape(y.shape[:-1] + (nxout,))
+
+
+def resample_table():
+    t = np.zeros(513 * 8, np.float32)
+    lib().rs_table(t)
+    return t.reshape(513, 8)
 
 
 def taylor(M):

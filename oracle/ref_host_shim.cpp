@@ -4,7 +4,8 @@
  * oracle/_ref/libref_host.so.  TEST INFRASTRUCTURE ONLY.
  *   - LSMOrCon_rec_2D.cpp (least-squares FD coefficients, Taylor order())
  *   - GPU_velocity_real.cpp (velocity file reader and ABC padding)
- * Both are included in place, unmodified, from the checkout's directory.
+ *   - Resample.cpp (trace resampling, 8-point sinc interpolation)
+ * All are included in place, unmodified, from the checkout's directory.
  */
 #include <cmath>
 #include <cstdio>
@@ -13,6 +14,7 @@
 
 #include "LSMOrCon_rec_2D.cpp"
 #include "GPU_velocity_real.cpp"
+#include "Resample.cpp"
 
 extern "C" {
 
@@ -51,6 +53,11 @@ void ref_velocity(char *path, float *v, float *v_2, float *r, float *r_1, float 
                   int N2, float tao, float h, int choice)
 {
     velocity(path, v, v_2, r, r_1, r_2, NZ, NX, NZ * NX, N2, tao, h, choice);
+}
+
+void ref_resample(int nxin, float dxin, float *yin, int nxout, float dxout, float *yout)
+{
+    resample(nxin, dxin, yin, nxout, dxout, yout);
 }
 
 } /* extern "C" */

@@ -13,14 +13,18 @@ LIB = os.path.join(LIBDIR, "librtm_gb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
-SOURCES = ["rtm_dropin.cu", "rtm_engine.cu", "rtm_host.cpp", "rtm_coeffs.cu", "rtm_noalloc.cu", "rtm_mlp.cu"]
+SOURCES = ["rtm_dropin.cu", "rtm_engine.cu", "rtm_host.cpp", "rtm_coeffs.cu", "rtm_noalloc.cu", "rtm_mlp.cu",
+           "rtm_io.cu"]
 # sources compiled without multiply-add contraction (FP64 parity with the host)
 NOFMA = {"rtm_coeffs.cu"}
 HEADERS = ["rtm_common.cuh", "rtm_engine_kernels.cuh"]
+# the reference-style executable (rtm_run_config on the run file in the cwd)
+CLI = os.path.join(LIBDIR, "rtm_gb300_run")
+CLI_SRC = "rtm_cli_main.cpp"
 
 
 def _newest_input() -> float:
-    paths = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
+    paths = [os.path.join(CSRC, f) for f in SOURCES + HEADERS + [CLI_SRC]]
     paths.append(os.path.join(HERE, "..", "include", "rtm_gb300.h"))
     return max(os.path.getmtime(p) for p in paths if os.path.exists(p))
 
@@ -37,7 +41,8 @@ def _compile(src: str) -> str:
 
 def build(force: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_input():
+    if (not force and os.path.exists(LIB) and os.path.exists(CLI)
+            and os.path.getmtime(LIB) >= _newest_input()):
         return LIB
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
@@ -47,6 +52,12 @@ def build(force: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    cmd = [NVCC, *ARCH, "-O2", "-std=c++17", "-o", CLI + ".tmp", os.path.join(CSRC, CLI_SRC),
+           "-L" + LIBDIR, "-lrtm_gb300", "-Xlinker", "-rpath=$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("executable link failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

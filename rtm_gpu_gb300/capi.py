@@ -100,6 +100,8 @@ def lib():
         L.rtm_ctx_set_kernel.argtypes = [vp, I, I, I]
         L.rtm_ctx_get_kernel.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.rtm_ctx_autotune.argtypes = [vp, I, ip, ip, ip, I, C.POINTER(C.c_double)]
+        L.rtm_resample.argtypes = [fp, I, I, C.c_float, fp, I, C.c_float, I]
+        L.rtm_run_config.argtypes = [C.c_char_p, I]
         _lib = L
     return _lib
 

@@ -90,8 +90,11 @@ struct rtm_ctx {
     float *img = nullptr, *ill = nullptr;
     CUtensorMap mapS[3], mapR[3];      // halo boxes of the rotating levels
     CUtensorMap flatS[3], flatR[3];    // flat tiles of the same buffers
-    CUtensorMap flatV;                 // flat tiles of the model (shared by the batch)
-    CUtensorMap flatVs;                // flat tiles of the per-shot window models
+    // per-cell model factors (v^2 tao^2/h^2 and velocity bin) of the model
+    // shared by the batch, and of the per-shot window models
+    float *mvv = nullptr, *mvvs = nullptr;
+    int *mbin = nullptr, *mbins = nullptr;
+    eng::ModelMaps mmaps, mmaps_s;
     // per-shot geometry of the current batch (device): padded width, window
     // start column in the survey interior, receiver start column
     int *gnx = nullptr, *gxa = nullptr, *grx0 = nullptr;
@@ -138,14 +141,14 @@ void free_all(rtm_ctx *c)
 {
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
-    float *fl[] = {c->v, c->r1, c->w, c->ctab, c->S[0], c->S[1], c->S[2], c->R[0], c->R[1], c->R[2],
+    float *fl[] = {c->mvv, c->mvvs, c->v, c->r1, c->w, c->ctab, c->S[0], c->S[1], c->S[2], c->R[0], c->R[1], c->R[2],
                    c->pre, c->rel1, c->rel2, c->sacc, c->racc, c->ring, c->data, c->rec, c->stage,
                    c->ups, c->downs, c->ks1, c->kc1, c->ks2, c->kc2, c->img, c->ill};
     for (float *p : fl)
         if (p) cudaFree(p);
     if (c->src) cudaFree(c->src);
     if (c->ctab4) cudaFree(c->ctab4);
-    for (int *q : {c->gnx, c->gxa, c->grx0, c->gitem})
+    for (int *q : {c->gnx, c->gxa, c->grx0, c->gitem, c->mbin, c->mbins})
         if (q) cudaFree(q);
     if (c->vs) cudaFree(c->vs);
     if (c->r1s) cudaFree(c->r1s);
@@ -184,7 +187,7 @@ int &pipe_grid()
 template <int MMAX, bool AD, int MODE>
 int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb)
 {
-    const CUtensorMap &fv = c->windowed ? c->flatVs : c->flatV;
+    const eng::ModelMaps &fv = c->windowed ? c->mmaps_s : c->mmaps;
     if (c->kv[MODE] == RTM_KERNEL_PERSISTENT) {
         const unsigned smem = eng::PipeSmem<MMAX, MODE>::BYTES;
         eng::k_step_pipe<MMAX, AD, MODE><<<pipe_grid<MMAX, AD, MODE>(), eng::NTHREADS, smem, c->st>>>(
@@ -454,6 +457,15 @@ int run_phase(rtm_ctx *c, int phase, int nb, int flags)
     return RTM_OK;
 }
 
+// Per-cell vv and bin of ncell model cells (kernel.cu's v*v*tao2*h2 and
+// int((v-vmin)/dv+0.5), formed once instead of at every step).
+void model_prep(rtm_ctx *c, const float *v, long long ncell, float *vv, int *bin)
+{
+    eng::k_model_prep<<<(unsigned)cdiv(ncell, 256), 256, 0, c->st>>>(
+        v, ncell, c->p.tao2, c->p.h2, c->p.vmin, c->p.dv, std::max(c->nbins, 1), vv,
+        c->p.adaptive ? bin : nullptr);
+}
+
 // Sets the per-shot geometry of the next batch: window start column xa and
 // interior width nx of each shot (NULL: the whole survey grid), sources in
 // each shot's own padded grid.  Windowed batches get their models and pad
@@ -508,7 +520,14 @@ int set_batch(rtm_ctx *c, int nb, const int *src_cells, const int *xa, const int
         if (int rc = dalloc(c, &c->r1s, bgrid)) return rc;
         if (int rc = dalloc(c, &c->meta_s, (size_t)nabc * c->B)) return rc;
         if (int rc = dalloc(c, &c->fac_s, (size_t)nabc * c->B)) return rc;
-        if (int rc = make_map(&c->flatVs, c->vs, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ)) return rc;
+        if (int rc = dalloc(c, &c->mvvs, bgrid)) return rc;
+        if (int rc = make_map(&c->mmaps_s.vv, c->mvvs, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ)) return rc;
+        if (c->p.adaptive) {
+            if (int rc = dalloc(c, &c->mbins, bgrid)) return rc;
+            if (int rc = make_map(&c->mmaps_s.bin, reinterpret_cast<float *>(c->mbins), c->NX, c->NZ, c->B,
+                                  c->P, eng::TX, eng::TZ))
+                return rc;
+        }
     }
     const long nabc = abc_count(c->NZ, c->NX, c->N2);
     eng::k_window_model<<<dim3(cdiv(c->ss, 256), nb), 256, 0, c->st>>>(
@@ -516,7 +535,8 @@ int set_batch(rtm_ctx *c, int nb, const int *src_cells, const int *xa, const int
     eng::k_pad_tables<<<dim3(cdiv(nabc, 256), nb), 256, 0, c->st>>>(
         c->vs, c->r1s, c->w, c->gnx, c->ss, nabc, c->NZ, c->P, c->N2, c->M, c->p.taoh, c->p.taoh2,
         c->p.quirk, c->meta_s, c->fac_s);
-    c->launches += 2;
+    model_prep(c, c->vs, (long long)c->ss * nb, c->mvvs, c->mbins);
+    c->launches += 3;
     RTM_LAUNCH_CHECK();
     return RTM_OK;
 }
@@ -655,9 +675,9 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     TRY(dalloc(c, &c->w, (size_t)c->N2 + 1));
     TRY(dalloc(c, &c->ctab, tab.size()));
     if (p->adaptive) {
-        // float4 groups: ctab4[q][bin] = c_{4q..4q+3}
-        const int Q = (c->MM + 4) / 4;
-        std::vector<float4> t4((size_t)Q * c->nbins);
+        // float4 groups (c_{4q..4q+3} of a bin) in the kernels' table layout
+        const int Q = eng::tab_groups(c->MM);
+        std::vector<float4> t4((size_t)eng::tab_pitch(c->MM) * c->nbins, make_float4(0.f, 0.f, 0.f, 0.f));
         for (int q = 0; q < Q; ++q)
             for (int b = 0; b < c->nbins; ++b) {
                 float g[4];
@@ -665,7 +685,7 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
                     const int l = 4 * q + k;
                     g[k] = l <= c->MM ? tab[(size_t)l * c->nbins + b] : 0.0f;
                 }
-                t4[(size_t)q * c->nbins + b] = make_float4(g[0], g[1], g[2], g[3]);
+                t4[eng::tab_index(q, b, c->nbins, c->MM)] = make_float4(g[0], g[1], g[2], g[3]);
             }
         TRY(dalloc(c, &c->ctab4, t4.size()));
         if (cudaMemcpy(c->ctab4, t4.data(), sizeof(float4) * t4.size(), cudaMemcpyHostToDevice) !=
@@ -716,8 +736,14 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
                 hv[(size_t)z * c->P + x] = p->v[(size_t)z * c->NX + xs];
                 hr[(size_t)z * c->P + x] = p->r1[(size_t)z * c->NX + xs];
             }
+        // the per-shot finishing scales by vmax snapped outward to the bin
+        // grid, as kernel.cu:717-720 leaves it before kernel.cu:947 uses it
         float vmx = p->v[0];
         for (long i = 0; i < (long)c->NZ * c->NX; ++i) vmx = std::max(vmx, p->v[i]);
+        if (p->dv > 0.0f) {
+            const float vel = (float)((int)(vmx / p->dv)) * p->dv;
+            vmx = (vel < vmx) ? vel + p->dv : vel;
+        }
         c->vmax = vmx;
         if (cudaMemcpy(c->v, hv.data(), grid * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(c->r1, hr.data(), grid * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -785,7 +811,19 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
         TRY(make_map(&c->flatS[i], c->S[i], c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
         TRY(make_map(&c->flatR[i], c->R[i], c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
     }
-    TRY(make_map(&c->flatV, c->v, c->NX, c->NZ, 1, c->P, eng::TX, eng::TZ));
+    TRY(dalloc(c, &c->mvv, (size_t)c->ss));
+    TRY(make_map(&c->mmaps.vv, c->mvv, c->NX, c->NZ, 1, c->P, eng::TX, eng::TZ));
+    if (c->p.adaptive) {
+        TRY(dalloc(c, &c->mbin, (size_t)c->ss));
+        TRY(make_map(&c->mmaps.bin, reinterpret_cast<float *>(c->mbin), c->NX, c->NZ, 1, c->P, eng::TX, eng::TZ));
+    }
+    model_prep(c, c->v, c->ss, c->mvv, c->mbin);
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) {
+        rtm_set_last_error("model preparation failed");
+        free_all(c);
+        delete c;
+        return RTM_ERR_CUDA;
+    }
     TRY(make_map(&c->imaps.rel1, c->rel1, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
     TRY(make_map(&c->imaps.rel2, c->rel2, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));
     TRY(make_map(&c->imaps.sacc, c->sacc, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ));

@@ -64,17 +64,27 @@ struct Shape {
 };
 
 // Shared-memory plan of k_step: halo boxes of the field(s) being advanced,
-// then flat tiles (u_{k-2} of each field, v, and the four imaging
-// accumulators in the backward step), then the mbarrier.
+// then flat tiles (u_{k-2} of each field, the per-cell factor v^2 tao^2/h^2,
+// the four imaging accumulators in the backward step, the per-cell velocity
+// bin), then the mbarrier.
 template <int MMAX, int MODE>
 struct Smem {
     static constexpr int NBOX = MODE == 1 ? 2 : 1;
-    static constexpr int NFLAT = MODE == 1 ? 7 : 2;  // fwd: a0, v; bwd: a0, s0, v, rel1, rel2, sacc, racc
+    // fwd: a0, vv, bin; bwd: a0, s0, vv, rel1, rel2, sacc, racc, bin (the bin
+    // tile is staged only with adaptive coefficients)
+    static constexpr int NFLAT = MODE == 1 ? 8 : 3;
     static constexpr unsigned BYTES = NBOX * Shape<MMAX>::BYTES + NFLAT * FLAT_BYTES + 16u;
 };
 
 struct ImgMaps {
     CUtensorMap rel1, rel2, sacc, racc;
+};
+
+// Per-cell model factors staged by the stencil kernels: vv = v^2 tao^2 / h^2
+// (float, kernel.cu's v*v*tao2*h2) and the velocity bin (int); one grid
+// shared by the batch or one per shot.
+struct ModelMaps {
+    CUtensorMap vv, bin;
 };
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
@@ -141,23 +151,34 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
     }
 }
 
-// Coefficients of one cell: the velocity bin (adaptive) picks a column of the
-// coefficient-major table; with fixed coefficients the table has one column
-// and the values are loaded once per warp into registers (cc).
+// Layout of the adaptive table: coefficient-major (float4 group q of bin b
+// at q*nbins + b) or bin-major (at b*QP + q, QP = groups rounded up to a
+// power of two, so one bin's coefficients fill one aligned 32/64-byte block).
+#ifndef RTM_TAB_BINMAJOR
+#define RTM_TAB_BINMAJOR 0
+#endif
+__host__ __device__ constexpr int tab_groups(int mmax) { return (mmax + 4) / 4; }
+__host__ __device__ constexpr int tab_pitch(int mmax) { return tab_groups(mmax) == 3 ? 4 : tab_groups(mmax); }
+__host__ __device__ __forceinline__ int tab_index(int q, int bin, int nbins, int mmax)
+{
+    return RTM_TAB_BINMAJOR ? bin * tab_pitch(mmax) + q : q * nbins + bin;
+}
+
+// Coefficients of one cell: the velocity bin (adaptive; precomputed per cell
+// as kernel.cu:55-57 forms it) picks a column of the coefficient-major table;
+// with fixed coefficients the values are loaded once into registers (cc).
 template <int MMAX, bool ADAPT>
-__device__ __forceinline__ void load_coefs(const StepArgs &a, float vc, const float *cc, float *cf)
+__device__ __forceinline__ void load_coefs(const StepArgs &a, int bin, const float *cc, float *cf)
 {
     if (!ADAPT) {
 #pragma unroll
         for (int l = 0; l <= MMAX; ++l) cf[l] = cc[l];
         return;
     }
-    int bin = (int)((vc - a.vmin) / a.dv + 0.5f);
-    bin = min(max(bin, 0), a.nbins - 1);
     constexpr int Q = (MMAX + 4) / 4;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const float4 g = __ldg(a.ctab4 + (long)q * a.nbins + bin);
+        const float4 g = __ldg(a.ctab4 + tab_index(q, bin, a.nbins, MMAX));
         if (4 * q + 0 <= MMAX) cf[4 * q + 0] = g.x;
         if (4 * q + 1 <= MMAX) cf[4 * q + 1] = g.y;
         if (4 * q + 2 <= MMAX) cf[4 * q + 2] = g.z;
@@ -185,6 +206,7 @@ __device__ __forceinline__ float lap_cell(const float *q, int C, const float *ro
 template <int MMAX, int MODE>
 struct Stage {
     float *tA, *tS, *fA0, *fV, *fS0, *fR1, *fR2, *fSa, *fRa;
+    int *fB;
     __device__ __forceinline__ explicit Stage(float *base)
     {
         using S = Shape<MMAX>;
@@ -194,27 +216,35 @@ struct Stage {
         fA0 = fl; fV = fl + FLAT;
         fS0 = fl + 2 * FLAT; fR1 = fl + 3 * FLAT; fR2 = fl + 4 * FLAT;
         fSa = fl + 5 * FLAT; fRa = fl + 6 * FLAT;
+        fB = reinterpret_cast<int *>(fl + (Smem<MMAX, MODE>::NFLAT - 1) * FLAT);
     }
 };
 
-// Stage bytes without the barrier word(s).
+// Stage bytes without the barrier word(s), and the bytes its copies bring
+// (no bin tile with fixed coefficients).
 template <int MMAX, int MODE>
 __host__ __device__ constexpr unsigned stage_bytes() { return Smem<MMAX, MODE>::BYTES - 16u; }
+template <int MMAX, int MODE, bool ADAPT>
+__host__ __device__ constexpr unsigned stage_tx_bytes()
+{
+    return stage_bytes<MMAX, MODE>() - (ADAPT ? 0u : FLAT_BYTES);
+}
 
 // TMA loads of one tile's inputs into a stage, completing on `bar`
 // (issued by one thread).
-template <int MMAX, int MODE>
+template <int MMAX, int MODE, bool ADAPT>
 __device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t *bar,
                                            const CUtensorMap &mapA, const CUtensorMap &mapS,
                                            const CUtensorMap &flatA0, const CUtensorMap &flatS0,
-                                           const CUtensorMap &flatV, const ImgMaps &img, int x0,
+                                           const ModelMaps &mod, const ImgMaps &img, int x0,
                                            int z0, int shot, int vshot)
 {
     using S = Shape<MMAX>;
-    mbar_arrive_expect_tx(bar, stage_bytes<MMAX, MODE>());
+    mbar_arrive_expect_tx(bar, stage_tx_bytes<MMAX, MODE, ADAPT>());
     tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
     tma_load_3d(st.fA0, &flatA0, x0, z0, shot, bar);
-    tma_load_3d(st.fV, &flatV, x0, z0, vshot ? shot : 0, bar);
+    tma_load_3d(st.fV, &mod.vv, x0, z0, vshot ? shot : 0, bar);
+    if (ADAPT) tma_load_3d(st.fB, &mod.bin, x0, z0, vshot ? shot : 0, bar);
     if (MODE == MODE_BWD) {
         tma_load_3d(st.tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, bar);
         tma_load_3d(st.fS0, &flatS0, x0, z0, shot, bar);
@@ -238,6 +268,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     using S = Shape<MMAX>;
     constexpr int QN = 2 * MMAX + 1;
     const float *tA = st.tA, *tS = st.tS, *fA0 = st.fA0, *fV = st.fV, *fS0 = st.fS0;
+    const int *fB = st.fB;
     const float *fR1 = st.fR1, *fR2 = st.fR2, *fSa = st.fSa, *fRa = st.fRa;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wx = warp % WX, wz = warp / WX;
@@ -248,7 +279,9 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     const int cx = S::XH + wx * 32 + lane;   // its column in the halo box
     const int rbase = wz * RW;               // box row of zw - MMAX
     const int fr = wz * RW * TX + wx * 32 + lane;  // flat-tile index of row zw
-    const int src_z = src / NX, src_x = src % NX;
+    // source row of this lane's column relative to the warp's first row (-1:
+    // the source is not in this column)
+    const int src_row = (src % NX == x0 + wx * 32 + lane) ? src / NX - (z0 + wz * RW) : -1;
     const int N2 = a.N2, NZ = a.NZ;
     const int rx0 = a.rx0s[shot];
     const bool col_in = gx >= N2 && gx < NX - N2;
@@ -260,7 +293,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     // issuing it early hides its latency behind the rows in between.
     float cfr[RW][MMAX + 1];
 #pragma unroll
-    for (int i = 0; i < PF; ++i) load_coefs<MMAX, ADAPT>(a, fV[fr + i * TX], cc, cfr[i]);
+    for (int i = 0; i < PF; ++i) load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + i * TX] : 0, cc, cfr[i]);
 
     if (MODE == MODE_FWD) {
         // two rows per iteration: two independent accumulation chains
@@ -272,7 +305,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #pragma unroll
             for (int h = 0; h < 2; ++h)
                 if (i + h + PF < RW)
-                    load_coefs<MMAX, ADAPT>(a, fV[fr + (i + h + PF) * TX], cc, cfr[i + h + PF]);
+                    load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + h + PF) * TX] : 0, cc, cfr[i + h + PF]);
             q[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
             q[QN] = tA[(rbase + i + QN) * S::BW + cx];
 #pragma unroll
@@ -280,12 +313,11 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
                 const int z = zw + i + h;
                 if (z >= NZ) continue;
                 const int t = fr + (i + h) * TX;
-                const float vc = fV[t];
                 const float *cf = cfr[i + h];
                 const float *row = tA + (rbase + i + h + MMAX) * S::BW + cx;
                 const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cf, a.k0, a.hzx2_1);
-                float val = fmaf(vc * vc * a.tao2 * a.h2, w1, 2.0f * q[MMAX + h] - fA0[t]);
-                if (z == src_z && gx == src_x) val += a.wavelet;
+                float val = fmaf(fV[t], w1, 2.0f * q[MMAX + h] - fA0[t]);
+                if (i + h == src_row) val += a.wavelet;
                 if (col_ok) {
                     const bool interior = col_in && z >= N2 && z < NZ - N2;
                     const long long g = g0 + (long)(i + h) * a.P;
@@ -318,14 +350,13 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     }
 #pragma unroll
     for (int i = 0; i < RW; ++i) {
-        if (i + PF < RW) load_coefs<MMAX, ADAPT>(a, fV[fr + (i + PF) * TX], cc, cfr[i + PF]);
+        if (i + PF < RW) load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + PF) * TX] : 0, cc, cfr[i + PF]);
         qr[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
         if (rows_s) qs[QN - 1] = tS[(rbase + i + QN - 1) * S::BW + cx];
         const int z = zw + i;
         if (z < NZ) {
             const int t = fr + i * TX;
-            const float vc = fV[t];
-            const float vv = vc * vc * a.tao2 * a.h2;
+            const float vv = fV[t];
             const float *cf = cfr[i];
             const float *rowR = tA + (rbase + i + MMAX) * S::BW + cx;
             const float *rowS = tS + (rbase + i + MMAX) * S::BW + cx;
@@ -364,7 +395,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
             }
             if (interior) {
                 float sv = fmaf(vv, ws, 2.0f * qs[MMAX] - fS0[t]);
-                if (z == src_z && gx == src_x) sv += a.wavelet;
+                if (i == src_row) sv += a.wavelet;
                 a.s2[g] = sv;
                 // imaging (kernel.cu:489-517)
                 if (a.compen) {
@@ -393,6 +424,9 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #ifndef RTM_FWD_PF
 #define RTM_FWD_PF 0
 #endif
+#ifndef RTM_BWD_PF
+#define RTM_BWD_PF 2
+#endif
 #ifndef RTM_PIPE_FWD_PF
 #define RTM_PIPE_FWD_PF 2
 #endif
@@ -404,11 +438,11 @@ template <int MMAX, bool ADAPT, int MODE>
 __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : RTM_FWD_MINB)
     k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
            const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
-           const __grid_constant__ CUtensorMap flatV, const __grid_constant__ ImgMaps img,
+           const __grid_constant__ ModelMaps mod, const __grid_constant__ ImgMaps img,
            const StepArgs a)
 {
     using SM = Smem<MMAX, MODE>;
-    constexpr int PF = MODE == MODE_FWD ? RTM_FWD_PF : (MMAX <= 8 ? 4 : 2);  // register budget
+    constexpr int PF = MODE == MODE_FWD ? RTM_FWD_PF : (MMAX <= 8 ? RTM_BWD_PF : 2);  // register budget
     extern __shared__ __align__(128) float smem[];
     const Stage<MMAX, MODE> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
@@ -421,7 +455,8 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         fence_barrier_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) issue_tile<MMAX, MODE>(st, &bar, mapA, mapS, flatA0, flatS0, flatV, img, x0, z0, shot, a.vshot);
+    if (threadIdx.x == 0)
+        issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot);
     // fixed coefficients: once per thread, while the copies are in flight
     float cc[MMAX + 1];
 #pragma unroll
@@ -466,7 +501,7 @@ template <int MMAX, bool ADAPT, int MODE>
 __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
     k_step_pipe(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
                 const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
-                const __grid_constant__ CUtensorMap flatV, const __grid_constant__ ImgMaps img,
+                const __grid_constant__ ModelMaps mod, const __grid_constant__ ImgMaps img,
                 const StepArgs a, const int *__restrict__ items, int nb)
 {
     constexpr int PF = MODE == MODE_BWD ? RW : RTM_PIPE_FWD_PF;
@@ -486,7 +521,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
     int shot, x0, z0;
     decode_item(items, nb, a.nxs, a.NZ, it, shot, x0, z0);
     if (threadIdx.x == 0)
-        issue_tile<MMAX, MODE>(st0, bar, mapA, mapS, flatA0, flatS0, flatV, img, x0, z0, shot, a.vshot);
+        issue_tile<MMAX, MODE, ADAPT>(st0, bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot);
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
@@ -502,8 +537,8 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
                 // the other stage was last read (and patched) in the previous
                 // iteration, which ended with a block barrier
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue_tile<MMAX, MODE>(s ? st0 : st1, bar + (s ^ 1), mapA, mapS, flatA0, flatS0, flatV,
-                                       img, nx0, nz0, nshot, a.vshot);
+                issue_tile<MMAX, MODE, ADAPT>(s ? st0 : st1, bar + (s ^ 1), mapA, mapS, flatA0, flatS0,
+                                              mod, img, nx0, nz0, nshot, a.vshot);
             }
         }
         const int NX = __ldg(a.nxs + shot);
@@ -799,6 +834,25 @@ __global__ void k_window_model(const float *vg, const float *r1g, int Pg, const 
 // Pad tables of each shot's grid (the device form of the table rtm_ctx_create
 // builds for a single grid): classification, inward directions, ring slot and
 // the model factors, from the shot's own padded model.
+// Per-cell model factors of nshot grids [shot][NZ][P]: vv = v*v*tao2*h2 in
+// the reference's float order, and the velocity bin int((v-vmin)/dv + 0.5)
+// with the 0.5 added in double as the reference's kernels do
+// (kernel.cu:56), clamped to the table.
+__global__ void k_model_prep(const float *__restrict__ v, long long ncell, float tao2, float h2,
+                             float vmin, float dv, int nbins, float *__restrict__ vv,
+                             int *__restrict__ bin)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncell) return;
+    const float x = v[i];
+    vv[i] = __fmul_rn(__fmul_rn(__fmul_rn(x, x), tao2), h2);
+    if (bin) {
+        const float q = __fdiv_rn(__fsub_rn(x, vmin), dv);
+        const int b = (int)((double)q + 0.5);
+        bin[i] = min(max(b, 0), nbins - 1);
+    }
+}
+
 __global__ void k_pad_tables(const float *vs, const float *r1s, const float *w, const int *nxs,
                              long long ss, long long tab_ss, int NZ, int P, int N2, int M,
                              float taoh, float taoh2, int quirk, int4 *meta, float4 *fac)

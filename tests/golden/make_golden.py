@@ -2,9 +2,9 @@
 
 Run in a checkout environment where caixh90/RTM_GPU's sources are available
 (oracle/build_ref.py compiles its kernel bodies, LSMOrCon_rec_2D.cpp,
-GPU_velocity_real.cpp and the Ricker function for the CPU):
+GPU_velocity_real.cpp, Resample.cpp and the Ricker function for the CPU):
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference] [--only name ...]
 
 Every array stored here was produced by the reference's code; the tests
 compare the oracle (and, through it, the GPU engine) against them.
@@ -236,16 +236,44 @@ def gen_shot(out):
     np.savez_compressed(os.path.join(out, "shot.npz"), **res)
 
 
+def gen_resample(out):
+    """Resample.cpp:193-225 on seeded traces for several interval ratios
+    (kernel.cu:839-845 resamples each trace from tao1 to tao)."""
+    L = orc.ref_host()
+    rng = np.random.default_rng(21)
+    res = {}
+    cases = [(101, 1.0, 0.33), (500, 0.002, 0.001), (400, 0.001, 0.0015), (300, 0.004, 0.001),
+             (64, 0.0005, 0.00025), (257, 0.001, 0.001), (33, 0.003, 0.0007)]
+    for i, (nxin, dxin, dxout) in enumerate(cases):
+        y = rng.standard_normal(nxin).astype(F32)
+        nxout = int((nxin - 1) * F32(dxin) / F32(dxout) + 1.5)  # kernel.cu:610 for NT
+        r = np.zeros(nxout, F32)
+        L.ref_resample(nxin, dxin, y, nxout, dxout, r)
+        res["case%d_param" % i] = np.array([nxin, dxin, dxout, nxout], np.float64)
+        res["case%d_in" % i] = y
+        res["case%d_out" % i] = r
+    np.savez_compressed(os.path.join(out, "resample.npz"), **res)
+
+
+GENERATORS = {"lsm": gen_lsm, "velocity_ricker": lambda o: gen_velocity_ricker(o),
+              "kernels": lambda o: gen_kernels(o), "shot": lambda o: gen_shot(o),
+              "resample": gen_resample}
+
+
 def main():
-    checkout = sys.argv[1] if len(sys.argv) > 1 else build_ref.DEFAULT_CHECKOUT
+    args = sys.argv[1:]
+    only = None
+    if "--only" in args:
+        i = args.index("--only")
+        only, args = args[i + 1:], args[:i]
+    checkout = args[0] if args else build_ref.DEFAULT_CHECKOUT
     got = build_ref.build_ref(checkout, force=True)
     if "host" not in got or "kernels" not in got:
         raise SystemExit("the reference's sources are needed to regenerate the fixtures")
     orc.set_threads(1)
-    gen_lsm(HERE)
-    gen_velocity_ricker(HERE)
-    gen_kernels(HERE)
-    gen_shot(HERE)
+    for name, gen in GENERATORS.items():
+        if only is None or name in only:
+            gen(HERE)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

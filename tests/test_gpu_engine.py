@@ -86,8 +86,10 @@ def test_graph_and_stepwise_agree(product_lib, cuda_ok):
     assert np.array_equal(a1, b1) and np.array_equal(a2, b2)
 
 
-def test_migrate_stack_matches_oracle(product_lib, cuda_ok):
-    p = small_problem(nx=100)
+@pytest.mark.parametrize("vhi", [1800.0, 1797.37])  # the second has a non-integer maximum
+def test_migrate_stack_matches_oracle(product_lib, cuda_ok, vhi):
+    p = small_problem(nx=100, vhi=vhi)
+    assert p.vmax >= float(p.v.max())  # snapped outward to the 1 m/s bin grid
     srcs = [p.src_flat(p.N2 + 1, p.N2 + x) for x in (10, 50, 90)]
     seis = np.stack([_seis(p, s) for s in range(len(srcs))])
     whitecoe = 1e-4

@@ -179,3 +179,14 @@ def test_live_oracle_vs_reference_random_problem():
     a1, a2 = orc.migrate(p, seis)
     b1, b2 = orc.migrate(p, seis, use_ref=True)
     assert np.array_equal(a1, b1) and np.array_equal(a2, b2)
+
+
+def test_resample_pins():
+    """Trace resampling (Resample.cpp:193-225) bit for bit."""
+    G = load("resample.npz")
+    n = len([k for k in G if k.endswith("_param")])
+    assert n >= 7
+    for i in range(n):
+        nxin, dxin, dxout, nxout = G["case%d_param" % i]
+        got = orc.resample(G["case%d_in" % i], np.float32(dxin), int(nxout), np.float32(dxout))
+        assert np.array_equal(got, G["case%d_out" % i]), i
