@@ -328,9 +328,39 @@ int rtm_resample(const float *yin, int ntrace, int nxin, float dxin, float *yout
  * shots on the batched engine (max_batch shots per launch, 0: 16) and writes
  * RVSP_RTM_up_<m>.dat / RVSP_RTM_down_<m>.dat per shot,
  * RVSP_Migration_Real_new2.dat and vnew.dat with the reference's names and
- * layouts.  The post-stack display chain that follows in the reference
- * (depth/time conversion, phase rotation, SEG-Y) is not part of this call. */
+ * layouts; for a full-depth output window also the reference's post-stack
+ * chain: RVSP_Migration_Real_T.dat (depth to time), _T_phase.dat (phase
+ * rotation by `angle`), _D.dat (back to depth) and RVSP_migration_Real.sgy
+ * (headers from SGY_Model.sgy in the working directory when present). */
 int rtm_run_config(const char *run_file, int max_batch);
+
+/* ======================================================================
+ * 6. The reference's post-stack display chain.
+ * ====================================================================== */
+
+/* DisToTimeAndTimeToDis1D.cpp:120-180 (D2T): traces img[ntr][nz] at depth
+ * step dz with velocities v[ntr][nz] to two-way time at dt: out[ntr][*nt].
+ * out may be NULL to query *nt; cap is out's capacity in floats.  flags:
+ * RTM_DEVICE_PTRS.  Bit-identical to the reference. */
+int rtm_depth_to_time(const float *v, const float *img, int ntr, int nz, float dz, float dt, float *out,
+                      long cap, int *nt, int flags);
+/* DisToTimeAndTimeToDis1D.cpp:30-118 (T2D): traces img[ntr][nt] at dt back
+ * to depth at dz with velocities v[ntr][nzv]: out[ntr][*nz]. */
+int rtm_time_to_depth(const float *v, int nzv, const float *img, int ntr, int nt, float dt, float dz,
+                      float *out, long cap, int *nz, int flags);
+/* phase_correction_ricker_decon.cpp:160-224 (phase_correction): every
+ * trace's spectrum rotated by angle degrees (FP64 FFT as the reference;
+ * traces up to 8192 samples). */
+int rtm_phase_rotate(const float *din, float *dout, int ntr, int nt, float angle, int flags);
+/* SGYWrite.cpp:3-55 (WriteSGY): ntr traces of ns samples to a SEG-Y file.
+ * With template_path the textual, binary and trace headers come from that
+ * file (the reference reads SGY_Model.sgy) and its sample format (IBM or
+ * IEEE) is kept; without it, blank headers and IEEE samples.  The binary
+ * header gets ns and the interval dt (seconds when < 1, else milliseconds;
+ * stored in microseconds); each trace header gets offset, sx, sy (per
+ * trace, may be NULL) and gx, gy. */
+int rtm_write_segy(const char *path, const char *template_path, const float *data, int ntr, int ns,
+                   float dt, const float *sx, const float *sy, float gx, float gy, const float *offset);
 
 #ifdef __cplusplus
 }

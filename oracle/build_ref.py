@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY.  Products:
 
 * ``oracle/_build/liboracle.so`` -- the C restatement (rtm_oracle.c,
-  lsm_oracle.c), FP32 + FP64, OpenMP.
+  lsm_oracle.c, resample_oracle.c, poststack_oracle.c), FP32 + FP64, OpenMP.
 * ``oracle/_ref/libref_rtm.so`` -- the reference's kernel bodies
   (caixh90/RTM_GPU kernel.cu:15-517) and Ricker function (kernel.cu:1261-1266)
   run on the CPU through ``ref_shim.cpp``.  The two source fragments are copied
@@ -13,6 +13,8 @@ TEST INFRASTRUCTURE ONLY.  Products:
 * ``oracle/_ref/libref_host.so`` -- LSMOrCon_rec_2D.cpp,
   GPU_velocity_real.cpp and Resample.cpp compiled in place from the checkout
   (only where the checkout exists; used to generate the golden fixtures).
+* ``oracle/_ref/libref_post.so`` -- DisToTimeAndTimeToDis1D.cpp and
+  phase_correction_ricker_decon.cpp, likewise (the post-stack chain).
 
 Everything is compiled with ``-ffp-contract=off`` so that neither x86-64 nor
 aarch64 fuses multiply-adds: the FP32 oracle then reproduces the reference's
@@ -49,10 +51,10 @@ def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     out = os.path.join(BUILD, "liboracle.so")
     srcs = [os.path.join(HERE, f) for f in
-            ("rtm_oracle.c", "lsm_oracle.c", "resample_oracle.c", "rtm_oracle_body.h",
-             "rtm_driver_body.h", "rtm_oracle.h")]
+            ("rtm_oracle.c", "lsm_oracle.c", "resample_oracle.c", "poststack_oracle.c",
+             "rtm_oracle_body.h", "rtm_driver_body.h", "rtm_oracle.h")]
     if force or _stale(out, srcs):
-        _run(["gcc", *CFLAGS, "-std=gnu11", "-o", out + ".tmp", srcs[0], srcs[1], srcs[2], "-lm"])
+        _run(["gcc", *CFLAGS, "-std=gnu11", "-o", out + ".tmp", *srcs[:4], "-lm"])
         os.replace(out + ".tmp", out)
     return out
 
@@ -100,6 +102,14 @@ def build_ref(checkout: str = DEFAULT_CHECKOUT, force: bool = False) -> dict:
             _run(["g++", *CFLAGS, "-w", "-I", checkout, "-o", out + ".tmp", srcs[0]])
             os.replace(out + ".tmp", out)
         got["host"] = out
+        out = os.path.join(REF_OUT, "libref_post.so")
+        srcs = [os.path.join(HERE, "ref_post_shim.cpp"),
+                os.path.join(checkout, "DisToTimeAndTimeToDis1D.cpp"),
+                os.path.join(checkout, "phase_correction_ricker_decon.cpp")]
+        if force or _stale(out, srcs):
+            _run(["g++", *CFLAGS, "-w", "-I", checkout, "-o", out + ".tmp", srcs[0]])
+            os.replace(out + ".tmp", out)
+        got["post"] = out
     return got
 
 

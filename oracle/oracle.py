@@ -29,6 +29,7 @@ class Params(C.Structure):
 
 _lib = None
 _ref = None
+_refp = None
 _refh = None
 
 
@@ -74,6 +75,12 @@ def lib():
                                      _i32p, _i32p, _i32p, C.c_void_p, C.c_int, C.c_double]
         L.ls_taylor.argtypes = [C.c_int, _f32p]
         L.or_resample.argtypes = [C.c_int, C.c_float, _f32p, C.c_int, C.c_float, _f32p]
+        L.or_d2t.restype = C.c_int
+        L.or_d2t.argtypes = [_f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_long]
+        L.or_t2d.restype = C.c_int
+        L.or_t2d.argtypes = [_f32p, C.c_int, _f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p,
+                             C.c_long]
+        L.or_phase.argtypes = [_f32p, _f32p, C.c_int, C.c_int, C.c_float]
         L.rs_table.argtypes = [_f32p]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_threads.restype = C.c_int
@@ -127,6 +134,26 @@ def ref_host():
         L.ref_resample.argtypes = [C.c_int, C.c_float, _f32p, C.c_int, C.c_float, _f32p]
         _refh = L
     return _refh
+
+
+def ref_post():
+    """DisToTimeAndTimeToDis1D.cpp / phase_correction_ricker_decon.cpp
+    compiled from the checkout."""
+    global _refp
+    if _refp is None:
+        got = _b.build_ref()
+        if "post" not in got:
+            raise RuntimeError("reference checkout unavailable")
+        L = C.CDLL(got["post"])
+        L.ref_d2t.restype = C.c_int
+        L.ref_d2t.argtypes = [C.c_char_p, _f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float,
+                              C.c_float, _f32p, C.c_long]
+        L.ref_t2d.restype = C.c_int
+        L.ref_t2d.argtypes = [C.c_char_p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_float,
+                              C.c_float, C.c_float, _f32p, C.c_long]
+        L.ref_phase_correction.argtypes = [_f32p, _f32p, C.c_int, C.c_int, C.c_float]
+        _refp = L
+    return _refp
 
 
 def set_threads(n: int) -> None:
@@ -291,6 +318,38 @@ def resample(y, dxin, nxout, dxout):
     for i in range(flat.shape[0]):
         lib().or_resample(flat.shape[1], dxin, np.ascontiguousarray(flat[i]), nxout, dxout, out[i])
     return out.reshape(y.shape[:-1] + (nxout,))
+
+
+def depth_to_time(v, img, dz, dt):
+    """DisToTimeAndTimeToDis1D.cpp (D2T): traces [ntr][nz] -> [ntr][nt]."""
+    v = np.ascontiguousarray(v, np.float32)
+    img = np.ascontiguousarray(img, np.float32)
+    ntr, nz = img.shape
+    nt = lib().or_d2t(v, img, ntr, nz, dz, dt, None, 0)
+    out = np.zeros((ntr, nt), np.float32)
+    assert lib().or_d2t(v, img, ntr, nz, dz, dt, out.ctypes.data_as(C.c_void_p), out.size) == nt
+    return out
+
+
+def time_to_depth(v, img_t, dt, dz):
+    """DisToTimeAndTimeToDis1D.cpp (T2D): v [ntr][nzv], traces [ntr][nt] ->
+    [ntr][nz]."""
+    v = np.ascontiguousarray(v, np.float32)
+    img_t = np.ascontiguousarray(img_t, np.float32)
+    ntr, nt = img_t.shape
+    nz = lib().or_t2d(v, v.shape[1], img_t, ntr, nt, dt, dz, None, 0)
+    out = np.zeros((ntr, nz), np.float32)
+    assert lib().or_t2d(v, v.shape[1], img_t, ntr, nt, dt, dz, out.ctypes.data_as(C.c_void_p),
+                        out.size) == nz
+    return out
+
+
+def phase_rotate(traces, angle):
+    """phase_correction_ricker_decon.cpp (phase_correction) on [ntr][nt]."""
+    d = np.ascontiguousarray(traces, np.float32)
+    out = np.zeros_like(d)
+    lib().or_phase(d, out, d.shape[0], d.shape[1], angle)
+    return out
 
 
 def resample_table():

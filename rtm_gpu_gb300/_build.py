@@ -14,7 +14,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
 SOURCES = ["rtm_dropin.cu", "rtm_engine.cu", "rtm_host.cpp", "rtm_coeffs.cu", "rtm_noalloc.cu", "rtm_mlp.cu",
-           "rtm_io.cu"]
+           "rtm_io.cu", "rtm_post.cu"]
 # sources compiled without multiply-add contraction (FP64 parity with the host)
 NOFMA = {"rtm_coeffs.cu"}
 HEADERS = ["rtm_common.cuh", "rtm_engine_kernels.cuh"]

@@ -102,6 +102,13 @@ def lib():
         L.rtm_ctx_autotune.argtypes = [vp, I, ip, ip, ip, I, C.POINTER(C.c_double)]
         L.rtm_resample.argtypes = [fp, I, I, C.c_float, fp, I, C.c_float, I]
         L.rtm_run_config.argtypes = [C.c_char_p, I]
+        L.rtm_depth_to_time.argtypes = [fp, fp, I, I, C.c_float, C.c_float, fp, C.c_long,
+                                        C.POINTER(C.c_int), I]
+        L.rtm_time_to_depth.argtypes = [fp, I, fp, I, I, C.c_float, C.c_float, fp, C.c_long,
+                                        C.POINTER(C.c_int), I]
+        L.rtm_phase_rotate.argtypes = [fp, fp, I, I, C.c_float, I]
+        L.rtm_write_segy.argtypes = [C.c_char_p, C.c_char_p, fp, I, I, C.c_float, fp, fp, C.c_float,
+                                     C.c_float, fp]
         _lib = L
     return _lib
 

@@ -343,7 +343,8 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     RTM_LAUNCH_CHECK();
     eng::StepArgs sa = base_step(c);
     eng::PadArgs pa = base_pad(c);
-    const long npad = abc_count(c->NZ, c->NX, c->N2) + (rec_on ? c->nrec : 0) + (r16 ? c->ringsz : 0);
+    const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT) + (rec_on ? c->nrec : 0) +
+                      (r16 ? c->ringsz : 0);
     const int kend = c->kstop ? std::min(c->kstop, NT) : NT;  // kstop-2 steps when tuning
     for (int k = 2; k < kend; ++k) {
         float *a0 = c->S[(k - 2) % 3], *a1 = c->S[(k - 1) % 3], *a2 = c->S[k % 3];
@@ -394,7 +395,7 @@ int enqueue_backward(rtm_ctx *c, int nb)
     sa.nrec = c->nrec;
     sa.dstride = (long long)NT * c->nrec;
     eng::PadArgs pa = base_pad(c);
-    const long npad = abc_count(c->NZ, c->NX, c->N2);
+    const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT);
     const int kend = c->kstop ? std::max(NT - c->kstop, 0) : 0;  // kstop-2 steps when tuning
     for (int k = NT - 3; k >= kend; --k) {
         const int i2 = k % 3, i1 = (k + 1) % 3, i0 = (k + 2) % 3;

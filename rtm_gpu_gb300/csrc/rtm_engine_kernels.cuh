@@ -232,20 +232,29 @@ __host__ __device__ constexpr unsigned stage_tx_bytes()
 
 // TMA loads of one tile's inputs into a stage, completing on `bar`
 // (issued by one thread).
+// Backward tiles without interior rows (the top and bottom pad bands) never
+// touch the source field or the imaging accumulators: those copies are
+// skipped.
+__device__ __forceinline__ bool tile_has_interior_rows(int z0, int NZ, int N2)
+{
+    return z0 + TZ > N2 && z0 < NZ - N2;
+}
+
 template <int MMAX, int MODE, bool ADAPT>
 __device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t *bar,
                                            const CUtensorMap &mapA, const CUtensorMap &mapS,
                                            const CUtensorMap &flatA0, const CUtensorMap &flatS0,
                                            const ModelMaps &mod, const ImgMaps &img, int x0,
-                                           int z0, int shot, int vshot)
+                                           int z0, int shot, int vshot, bool with_s)
 {
     using S = Shape<MMAX>;
-    mbar_arrive_expect_tx(bar, stage_tx_bytes<MMAX, MODE, ADAPT>());
+    const unsigned skip = (MODE == MODE_BWD && !with_s) ? S::BYTES + 5u * FLAT_BYTES : 0u;
+    mbar_arrive_expect_tx(bar, stage_tx_bytes<MMAX, MODE, ADAPT>() - skip);
     tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
     tma_load_3d(st.fA0, &flatA0, x0, z0, shot, bar);
     tma_load_3d(st.fV, &mod.vv, x0, z0, vshot ? shot : 0, bar);
     if (ADAPT) tma_load_3d(st.fB, &mod.bin, x0, z0, vshot ? shot : 0, bar);
-    if (MODE == MODE_BWD) {
+    if (MODE == MODE_BWD && with_s) {
         tma_load_3d(st.tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, bar);
         tma_load_3d(st.fS0, &flatS0, x0, z0, shot, bar);
         tma_load_3d(st.fR1, &img.rel1, x0, z0, shot, bar);
@@ -455,8 +464,10 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         fence_barrier_init();
     }
     __syncthreads();
+    const bool with_s = tile_has_interior_rows(z0, a.NZ, a.N2);
     if (threadIdx.x == 0)
-        issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot);
+        issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
+                                      with_s);
     // fixed coefficients: once per thread, while the copies are in flight
     float cc[MMAX + 1];
 #pragma unroll
@@ -464,7 +475,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
     if (ok) {
         patch_halo<MMAX>(st.tA, x0, z0, NX, a.NZ);
-        if (MODE == MODE_BWD) patch_halo<MMAX>(st.tS, x0, z0, NX, a.NZ);
+        if (MODE == MODE_BWD && with_s) patch_halo<MMAX>(st.tS, x0, z0, NX, a.NZ);
     }
     if (!__syncthreads_and(ok)) {
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
@@ -521,7 +532,8 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
     int shot, x0, z0;
     decode_item(items, nb, a.nxs, a.NZ, it, shot, x0, z0);
     if (threadIdx.x == 0)
-        issue_tile<MMAX, MODE, ADAPT>(st0, bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot);
+        issue_tile<MMAX, MODE, ADAPT>(st0, bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
+                                      tile_has_interior_rows(z0, a.NZ, a.N2));
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
@@ -538,14 +550,16 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
                 // iteration, which ended with a block barrier
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 issue_tile<MMAX, MODE, ADAPT>(s ? st0 : st1, bar + (s ^ 1), mapA, mapS, flatA0, flatS0,
-                                              mod, img, nx0, nz0, nshot, a.vshot);
+                                              mod, img, nx0, nz0, nshot, a.vshot,
+                                              tile_has_interior_rows(nz0, a.NZ, a.N2));
             }
         }
         const int NX = __ldg(a.nxs + shot);
         const bool ok = mbar_wait_bounded(bar + s, (phase >> s) & 1u, &g_rtm_dev_error);
         if (ok) {
             patch_halo<MMAX>(cur.tA, x0, z0, NX, a.NZ);
-            if (MODE == MODE_BWD) patch_halo<MMAX>(cur.tS, x0, z0, NX, a.NZ);
+            if (MODE == MODE_BWD && tile_has_interior_rows(z0, a.NZ, a.N2))
+                patch_halo<MMAX>(cur.tS, x0, z0, NX, a.NZ);
         }
         if (!__syncthreads_and(ok)) {
             // let the copies in flight land before the CTA exits
@@ -664,14 +678,50 @@ __host__ __device__ __forceinline__ int4 pad_meta(long t, int NZ, int NX, int P,
 // corner: b = inv*(u1[c] + r_1*(u2[c+dx]+u2[c+dz])); u2 is read before
 // blending (pre-blend pad values from `pre`, interior values from a2);
 // out = (1-w)*u2[c] + w*b.
+#ifndef RTM_PAD_CPT
+#define RTM_PAD_CPT 2
+#endif
+constexpr int PAD_CPT = RTM_PAD_CPT;  // pad cells per thread
+
+// The update of pad cell t of one shot, without branches on its kind: a
+// corner cell reads its side-cell operands at zero lateral offset (valid
+// addresses) and the corner formula is selected at the end, so the loads of
+// several cells of a thread can all be in flight together.
+struct PadOut {
+    float out;
+    long c, ri;
+};
+
+__device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long so, long t)
+{
+    const int4 m = __ldg(a.meta + shot * a.tab_ss + t);
+    const float4 f = __ldg(a.fac + shot * a.tab_ss + t);
+    const bool corner = m.w & 1;
+    const long c = m.x, n = c + m.y, sd = corner ? 0 : m.z, zc = corner ? m.z : 0;
+    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so;
+    const float u2n = pr[n], pnp = pr[n + sd], pnm = pr[n - sd], pcz = pr[c + zc], pc = pr[c];
+    const float u0c = u0[c], u0n = u0[n], u0p = u0[c + sd], u0m = u0[c - sd];
+    const float u1c = u1[c], u1n = u1[n];
+    const float lat = pnp - 2.0f * u2n + pnm + u0p - 2.0f * u0c + u0m;
+    const float bs = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1c + u0c + u2n - 2.0f * u1n + u0n) +
+                            f.z * lat);
+    const float bc = f.y * (u1c + f.x * (u2n + pcz));
+    PadOut r;
+    r.out = (1.0f - f.w) * pc + f.w * (corner ? bc : bs);
+    r.c = c;
+    r.ri = a.ring_mode ? (long)(m.w >> 1) - 1 : -1;
+    return r;
+}
+
 __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y;
     const long long so = (long long)shot * a.ss;
     const int NX = a.nxs[shot];
-    if (t >= a.nabc) {
-        long j = t - a.nabc;
+    const long npadt = (a.nabc + PAD_CPT - 1) / PAD_CPT;  // threads of the pad cells
+    if (t >= npadt) {
+        long j = t - npadt;
         if (a.rec && j < a.nrec) {
             const int z = a.rz0 + (int)j * a.rdz, x = a.rx0s[shot] + (int)j * a.rdx;
             a.rec[(long long)shot * a.rec_ss + j] = a.a1[so + (long)z * a.P + x];
@@ -687,38 +737,35 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         }
         return;
     }
-    if (t >= abc_count(a.NZ, NX, a.N2)) return;  // this shot's pad is smaller
-    // Neighbour values of level k before blending come from `pre`, which the
-    // stencil kernel fills for every pad cell and the first interior ring.
-    const int4 m = __ldg(a.meta + shot * a.tab_ss + t);
-    const float4 f = __ldg(a.fac + shot * a.tab_ss + t);
-    const long c = m.x;
-    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so;
-    float b;
-    if (!(m.w & 1)) {
-        const long n = c + m.y, sd = m.z;
-        const float u2n = pr[n];
-        const float u0c = u0[c], u0n = u0[n];
-        const float lat = pr[n + sd] - 2.0f * u2n + pr[n - sd] + u0[c + sd] - 2.0f * u0c + u0[c - sd];
-        b = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1[c] + u0c + u2n - 2.0f * u1[n] + u0n) +
-                   f.z * lat);
-    } else {
-        b = f.y * (u1[c] + f.x * (pr[c + m.y] + pr[c + m.z]));
+    const long nmine = abc_count(a.NZ, NX, a.N2);  // this shot's pad may be smaller
+    PadOut r[PAD_CPT];
+    bool on[PAD_CPT];
+#pragma unroll
+    for (int k = 0; k < PAD_CPT; ++k) {
+        const long tk = t * PAD_CPT + k;
+        on[k] = tk < nmine;
+        if (on[k]) r[k] = pad_cell(a, shot, so, tk);
     }
-    const float out = (1.0f - f.w) * pr[c] + f.w * b;
-    a.a2[so + c] = out;
-    const long ri = a.ring_mode ? (long)(m.w >> 1) - 1 : -1;
-    if (ri >= 0) {
-        if (a.ring_prec == 0) {
-            if (a.ring_mode == 1)
-                a.ring[(long long)shot * a.ring_ss + ri] = out;
-            else
-                a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + ri];
-        } else if (a.ring_mode == 1) {
-            a.stage[(long long)shot * a.ringsz + ri] = out;
-        } else {
-            const long long sl = (long long)shot * a.slots + a.slot;
-            a.s2[so + c] = ring_dequant(a.ring16[sl * a.ringsz + ri], a.scale[sl], a.ring_prec);
+    unsigned bits = 0u;
+#pragma unroll
+    for (int k = 0; k < PAD_CPT; ++k) {
+        if (!on[k]) continue;
+        const long c = r[k].c, ri = r[k].ri;
+        const float out = r[k].out;
+        a.a2[so + c] = out;
+        if (ri >= 0) {
+            if (a.ring_prec == 0) {
+                if (a.ring_mode == 1)
+                    a.ring[(long long)shot * a.ring_ss + ri] = out;
+                else
+                    a.s2[so + c] = a.ring[(long long)shot * a.ring_ss + ri];
+            } else if (a.ring_mode == 1) {
+                a.stage[(long long)shot * a.ringsz + ri] = out;
+                bits = max(bits, __float_as_uint(fabsf(out)));
+            } else {
+                const long long sl = (long long)shot * a.slots + a.slot;
+                a.s2[so + c] = ring_dequant(a.ring16[sl * a.ringsz + ri], a.scale[sl], a.ring_prec);
+            }
         }
     }
     if (a.ring_prec && a.ring_mode == 1) {
@@ -726,7 +773,7 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         // lanes of a block belong to one shot), one atomic per warp.  Float
         // bits of non-negative values order like unsigned integers.
         const unsigned mask = __activemask();
-        const unsigned bits = __reduce_max_sync(mask, ri >= 0 ? __float_as_uint(fabsf(out)) : 0u);
+        bits = __reduce_max_sync(mask, bits);
         if ((threadIdx.x & 31) == __ffs(mask) - 1 && bits)
             atomicMax(a.amax + (long long)shot * a.slots + a.slot, bits);
     }

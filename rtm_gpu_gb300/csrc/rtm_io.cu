@@ -272,7 +272,7 @@ int rtm_run_config(const char *run_file, int max_batch)
     sc.line(); dpr_file = sc.token();
     sc.line(); para_file = sc.token();
     sc.line(); result = sc.token();
-    (void)Nsmooth; (void)wthite_phase; (void)angle;  // post-stack display settings
+    (void)Nsmooth; (void)wthite_phase;  // read by the reference, not used by its chain
     if (!sc.ok) return fail("run file: missing entries");
     // ---- parameter file (kernel.cu:603-605)
     Scanner ps;
@@ -427,7 +427,47 @@ int rtm_run_config(const char *run_file, int max_batch)
     if (!write_floats(result + "RVSP_Migration_Real_new2.dat", out.data(), out.size()) ||
         !write_floats(result + "vnew.dat", vout.data(), vout.size()))
         return fail("cannot write the stacked image", RTM_ERR_IO);
-    return RTM_OK;
+    // ---- post-stack display chain (kernel.cu:1108-1196).  The reference
+    // reads the two files back as NX_ED-NX_BG traces of mod_NZ samples each
+    // (a flat read, whatever their row count); it only makes sense, and is
+    // only run here, for a full-depth window.
+    if (NZ_BG != 0 || NZ_ED != mod_NZ) return RTM_OK;
+    const int ntr = NX_ED - NX_BG;
+    std::vector<float> img2((size_t)ntr * mod_NZ, 0.0f), vdt((size_t)ntr * mod_NZ, 0.0f);
+    std::memcpy(img2.data(), out.data(), sizeof(float) * std::min(out.size(), img2.size()));
+    std::memcpy(vdt.data(), vout.data(), sizeof(float) * std::min(vout.size(), vdt.size()));
+    for (float x : vdt)
+        if (!(x > 0.0f)) return fail("velocity window of the post-stack chain is not positive");
+    int nt = 0;
+    if ((rc = rtm_depth_to_time(vdt.data(), img2.data(), ntr, mod_NZ, hz, tao, nullptr, 0, &nt, 0))) return rc;
+    std::vector<float> mt((size_t)ntr * nt), mtp((size_t)ntr * nt);
+    if ((rc = rtm_depth_to_time(vdt.data(), img2.data(), ntr, mod_NZ, hz, tao, mt.data(), (long)mt.size(), &nt, 0)))
+        return rc;
+    if (!write_floats(result + "RVSP_Migration_Real_T.dat", mt.data(), mt.size()))
+        return fail("cannot write the time image", RTM_ERR_IO);
+    if ((rc = rtm_phase_rotate(mt.data(), mtp.data(), ntr, nt, angle, 0))) return rc;
+    if (!write_floats(result + "RVSP_Migration_Real_T_phase.dat", mtp.data(), mtp.size()))
+        return fail("cannot write the phase-rotated image", RTM_ERR_IO);
+    int nzd = 0;
+    if ((rc = rtm_time_to_depth(vdt.data(), mod_NZ, mtp.data(), ntr, nt, tao, hz, nullptr, 0, &nzd, 0)))
+        return rc;
+    std::vector<float> md((size_t)ntr * std::max(nzd, 1));
+    if ((rc = rtm_time_to_depth(vdt.data(), mod_NZ, mtp.data(), ntr, nt, tao, hz, md.data(), (long)md.size(),
+                                &nzd, 0)))
+        return rc;
+    if (!write_floats(result + "RVSP_Migration_Real_D.dat", md.data(), (size_t)ntr * nzd))
+        return fail("cannot write the depth image", RTM_ERR_IO);
+    // SEG-Y of the stacked depth image (SGYWrite.cpp, called at kernel.cu:1190)
+    std::vector<float> sx(ntr), sy(ntr), dsr(ntr);
+    for (int i = 0; i < ntr; ++i) {
+        sx[i] = 1.0f * i * 10;
+        sy[i] = -1.0f * i * 10;
+        dsr[i] = 1000 - i;
+    }
+    FILE *tp = std::fopen("SGY_Model.sgy", "rb");
+    if (tp) std::fclose(tp);
+    return rtm_write_segy((result + "RVSP_migration_Real.sgy").c_str(), tp ? "SGY_Model.sgy" : nullptr,
+                          img2.data(), ntr, mod_NZ, (float)(int)hz, sx.data(), sy.data(), 1.0f, 1.0f, dsr.data());
 }
 
 }  // extern "C"

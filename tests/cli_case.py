@@ -106,4 +106,23 @@ def oracle_outputs(c, vin, gathers):
     else:
         out["RVSP_Migration_Real_new2.dat"] = img[BG:ED, ZB:ZE]
         out["vnew.dat"] = np.stack([v[ZB:ZE + N2, j] for j in range(BG + N2, ED + N2)])
+    if ZB == 0 and ZE == nz:
+        # post-stack chain (kernel.cu:1108-1196): both files read back flat as
+        # ED-BG traces of nz samples
+        ntr = ED - BG
+
+        def flat(a):
+            f = np.zeros(ntr * nz, np.float32)
+            a = a.ravel()[:ntr * nz]
+            f[:a.size] = a
+            return f.reshape(ntr, nz)
+
+        mig, vdt = flat(out["RVSP_Migration_Real_new2.dat"]), flat(out["vnew.dat"])
+        hz = np.float32(c["hz"])
+        t = orc.depth_to_time(vdt, mig, hz, np.float32(tao))
+        tp = orc.phase_rotate(t, float(c["angle"]))
+        out["RVSP_Migration_Real_T.dat"] = t
+        out["RVSP_Migration_Real_T_phase.dat"] = tp
+        out["RVSP_Migration_Real_D.dat"] = orc.time_to_depth(vdt, tp, np.float32(tao), hz)
+        out["RVSP_migration_Real.sgy"] = mig
     return out, NT

@@ -2,7 +2,8 @@
 
 Run in a checkout environment where caixh90/RTM_GPU's sources are available
 (oracle/build_ref.py compiles its kernel bodies, LSMOrCon_rec_2D.cpp,
-GPU_velocity_real.cpp, Resample.cpp and the Ricker function for the CPU):
+GPU_velocity_real.cpp, Resample.cpp, DisToTimeAndTimeToDis1D.cpp,
+phase_correction_ricker_decon.cpp and the Ricker function for the CPU):
 
     python tests/golden/make_golden.py [/path/to/reference] [--only name ...]
 
@@ -255,9 +256,53 @@ def gen_resample(out):
     np.savez_compressed(os.path.join(out, "resample.npz"), **res)
 
 
+def poststack_inputs(seed=31, ntr=48, nz=700):
+    """Seeded image traces and depth velocities of the post-stack pins (the
+    pin test regenerates them)."""
+    rng = np.random.default_rng(seed)
+    v = np.sort((2000.0 + rng.uniform(0, 2500, (ntr, nz))).astype(F32), axis=1)
+    img = rng.standard_normal((ntr, nz)).astype(F32)
+    return v, img
+
+
+def gen_poststack(out):
+    """D2T, T2D and phase_correction of the reference on seeded traces.
+    The outputs are stored as SHA-256 digests (plus short slices): the
+    arrays are large and the pins are bit-for-bit.  The sizes keep the
+    reference's work arrays above the allocator's mmap threshold, so the
+    entry it reads uninitialised is zero."""
+    import hashlib
+    # fixed mmap threshold (no dynamic growth): the reference's work arrays
+    # then come from fresh zero-filled pages whatever this process freed before
+    C.CDLL("libc.so.6").mallopt(-3, 64 * 1024)  # M_MMAP_THRESHOLD
+    L = orc.ref_post()
+    v, img = poststack_inputs()
+    ntr, nz = img.shape
+    dz, dt = 5.0, 0.003
+    scratch = os.path.join(tempfile.mkdtemp(), "post.bin").encode()
+    buf = np.zeros(ntr * 20000, F32)
+    nt = L.ref_d2t(scratch, v, img, ntr, nz, dz, dz, dt, buf, buf.size)
+    t = buf[:ntr * nt].reshape(ntr, nt).copy()
+    buf2 = np.zeros(ntr * 20000, F32)
+    nz2 = L.ref_t2d(scratch, v, t, ntr, nt, nz, dz, dt, dz, buf2, buf2.size)
+    d = buf2[:ntr * nz2].reshape(ntr, nz2).copy()
+    res = {"params": np.array([31, ntr, nz, dz, dt, nt, nz2], np.float64)}
+    res["d2t_sha"] = np.frombuffer(hashlib.sha256(t.tobytes()).digest(), np.uint8)
+    res["t2d_sha"] = np.frombuffer(hashlib.sha256(d.tobytes()).digest(), np.uint8)
+    res["d2t_slice"] = t[:2, :64].copy()
+    res["t2d_slice"] = d[:2, :64].copy()
+    for i, ang in enumerate((90.0, 37.5, -60.0)):
+        ph = np.zeros_like(t)
+        L.ref_phase_correction(t, ph, ntr, nt, ang)
+        res["phase%d_angle" % i] = np.array([ang])
+        res["phase%d_sha" % i] = np.frombuffer(hashlib.sha256(ph.tobytes()).digest(), np.uint8)
+        res["phase%d_slice" % i] = ph[:2, :64].copy()
+    np.savez_compressed(os.path.join(out, "poststack.npz"), **res)
+
+
 GENERATORS = {"lsm": gen_lsm, "velocity_ricker": lambda o: gen_velocity_ricker(o),
               "kernels": lambda o: gen_kernels(o), "shot": lambda o: gen_shot(o),
-              "resample": gen_resample}
+              "resample": gen_resample, "poststack": gen_poststack}
 
 
 def main():
@@ -268,7 +313,7 @@ def main():
         only, args = args[i + 1:], args[:i]
     checkout = args[0] if args else build_ref.DEFAULT_CHECKOUT
     got = build_ref.build_ref(checkout, force=True)
-    if "host" not in got or "kernels" not in got:
+    if "host" not in got or "kernels" not in got or "post" not in got:
         raise SystemExit("the reference's sources are needed to regenerate the fixtures")
     orc.set_threads(1)
     for name, gen in GENERATORS.items():

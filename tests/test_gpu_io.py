@@ -58,7 +58,8 @@ def _run_cli(d):
 
 
 @pytest.mark.parametrize("kw", [dict(), dict(iLSTE=1, ifv=1, iNorm=0, iCompen=0),
-                                dict(tao1=0.002, NT1=81)])  # last: gathers resampled 2 ms -> 1 ms
+                                dict(tao1=0.002, NT1=81),   # gathers resampled 2 ms -> 1 ms
+                                dict(NZ_BG=0, NZ_ED=40, angle=90.0)])  # + the post-stack chain
 def test_reference_run_directory(product_lib, cuda_ok, tmp_path, kw):
     """The reference's run directory through rtm_gb300_run, file for file
     against the oracle run of the same flow."""
@@ -69,7 +70,16 @@ def test_reference_run_directory(product_lib, cuda_ok, tmp_path, kw):
     exp, NT = cli_case.oracle_outputs(c, vin, gathers)
     _run_cli(str(tmp_path))
     for name, e in exp.items():
-        got = np.fromfile(os.path.join(tmp_path, c["Result"], name), np.float32)
+        path = os.path.join(tmp_path, c["Result"], name)
+        if name.endswith(".sgy"):
+            b = open(path, "rb").read()
+            ntr, ns = e.shape
+            assert len(b) == 3600 + ntr * (240 + 4 * ns)
+            got = np.stack([np.frombuffer(b[3600 + i * (240 + 4 * ns) + 240:3600 + (i + 1) * (240 + 4 * ns)],
+                                          ">f4") for i in range(ntr)])
+            assert rel_l2(got, e) < 1e-3
+            continue
+        got = np.fromfile(path, np.float32)
         assert got.size == e.size, name
         got = got.reshape(e.shape)
         if name == "vnew.dat":
@@ -77,3 +87,5 @@ def test_reference_run_directory(product_lib, cuda_ok, tmp_path, kw):
         else:
             tol = 1e-3 if name.startswith("RVSP_Migration") else 1e-4
             assert rel_l2(got, e) < tol, (name, rel_l2(got, e))
+    if c["NZ_BG"] != 0 or c["NZ_ED"] != c["mod_NZ"]:  # the chain runs only for a full-depth window
+        assert not os.path.exists(os.path.join(tmp_path, c["Result"], "RVSP_Migration_Real_T.dat"))

@@ -190,3 +190,26 @@ def test_resample_pins():
         nxin, dxin, dxout, nxout = G["case%d_param" % i]
         got = orc.resample(G["case%d_in" % i], np.float32(dxin), int(nxout), np.float32(dxout))
         assert np.array_equal(got, G["case%d_out" % i]), i
+
+
+def test_poststack_pins():
+    """D2T / T2D / phase_correction (the reference's post-stack chain) bit
+    for bit on the seeded traces of the fixture."""
+    import hashlib
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden import poststack_inputs
+    G = load("poststack.npz")
+    seed, ntr, nz, dz, dt, nt, nz2 = G["params"]
+    v, img = poststack_inputs(int(seed), int(ntr), int(nz))
+    t = orc.depth_to_time(v, img, np.float32(dz), np.float32(dt))
+    assert t.shape == (int(ntr), int(nt))
+    assert np.array_equal(t[:2, :64], G["d2t_slice"])
+    assert hashlib.sha256(t.tobytes()).digest() == G["d2t_sha"].tobytes()
+    d = orc.time_to_depth(v, t, np.float32(dt), np.float32(dz))
+    assert d.shape == (int(ntr), int(nz2))
+    assert hashlib.sha256(d.tobytes()).digest() == G["t2d_sha"].tobytes()
+    for i in range(3):
+        ph = orc.phase_rotate(t, float(G["phase%d_angle" % i][0]))
+        assert np.array_equal(ph[:2, :64], G["phase%d_slice" % i])
+        assert hashlib.sha256(ph.tobytes()).digest() == G["phase%d_sha" % i].tobytes()
