@@ -60,10 +60,11 @@ def parse():
     ap.add_argument("--cpu-sample-nt", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split"],
                     help="stencil kernel form (auto: the autotuner picks it and shots per launch)")
-    ap.add_argument("--workload", default="multishot", choices=["multishot", "rvsp"],
-                    help="rvsp: batched uneven aperture windows, well receivers, autotuned")
+    ap.add_argument("--workload", default="multishot", choices=["multishot", "rvsp", "c5"],
+                    help="rvsp: batched uneven aperture windows, well receivers, autotuned; "
+                         "c5: learned coefficients, 1201x4001 model, BF16 rings, uneven apertures")
     return ap.parse_args()
 
 
@@ -289,7 +290,8 @@ def run_rvsp(a, cfg):
     if a.kernel == "auto":
         tuned = eng.autotune(wsrc, xa, wn, nsteps=20)
     else:
-        v = capi.RTM_KERNEL_TILED if a.kernel == "tiled" else capi.RTM_KERNEL_PERSISTENT
+        v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
+             "split": capi.RTM_KERNEL_SPLIT}[a.kernel]
         eng.set_kernel(v, v)
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
@@ -335,8 +337,8 @@ def run_rvsp(a, cfg):
                                    % (cfg.nz, cfg.nx, nshot, rec[4], 50 + rec[4] - 1, cfg.NT,
                                       cfg.M, cfg.coef, cfg.ring.upper()),
                        "shots": nshot, "mean_window": float(np.mean(wn)), "batch": batch,
-                       "autotuned": {"fwd_kernel": ["tiled", "persistent"][kern["fwd"]],
-                                     "bwd_kernel": ["tiled", "persistent"][kern["bwd"]],
+                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split"][kern["fwd"]],
+                                     "bwd_kernel": ["tiled", "persistent", "tiled-split"][kern["bwd"]],
                                      "shots_per_launch": kern["shots_per_launch"],
                                      "tuning_gcells_per_s": tuned},
                        "l2": "inputs larger than L2 (%.1f GB of wavefields and rings)"
@@ -351,6 +353,125 @@ def run_rvsp(a, cfg):
     eng.close()
 
 
+def run_c5(a, cfg):
+    """Learned coefficients plus the full stack on the 1201x4001 model
+    (dx=dz=10 m, 1500-6000 m/s gradients with salt-like 4500 m/s bodies):
+    the coefficient table comes from the MLP trained on the GPU on FP64
+    optimiser samples of the survey's (r, kh) range, with the optimiser as
+    fallback wherever the network's dispersion error exceeds 1e-4; shots with
+    uneven aperture windows, BF16 rings, autotuned kernels.  The shot count
+    and steps are reduced from the 256 x 8000 of the full configuration
+    (--shots / --nt) so the run fits a few minutes."""
+    import torch
+    from rtm_gpu_gb300 import Engine, capi, coeffs, mlp, synth
+    from rtm_gpu_gb300.problem import build_problem, f32
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    nz, nx, N2, h, tao, f0, M = 1201, 4001, 30, 10.0, 0.001, 25.0, 8
+    nshot = a.shots if a.shots != 64 else 8
+    nt = a.nt if a.nt != 4000 else 8000
+    vtrue = synth.model_c5(nz=nz, nx=nx)
+    vmig = synth.smooth_model(vtrue, 10.0)
+    fmax = 2 * f0
+    vlo, vhi = float(vmig.min()), float(vmig.max())
+    t0 = time.perf_counter()
+    net, train_loss = mlp.train_default(n=50000, epochs=60, seed=5, batch=512, lr=3e-3,
+                                        r_range=(vlo * tao / h * 0.98, vhi * tao / h * 1.02),
+                                        kh_range=(2 * np.pi * fmax * h / vhi * 0.98,
+                                                  2 * np.pi * fmax * h / vlo * 1.02),
+                                        m_range=(M, M))
+    t_train = time.perf_counter() - t0
+    info_box = {}
+
+    def table(vmin, dv, nvel, need, hzx):
+        assert dv == 1.0
+        length, index, coef, info = net.table(M=M, tol=1e-4, tao=tao, h=h, fmax=fmax, vmin=vmin,
+                                              nvel=nvel, need=need)
+        info_box.update(info)
+        return length, index, coef
+
+    # surface receivers on interior columns 1500..2499, common to every
+    # window; windows of seeded widths 1500..4001 placed to contain them
+    rec = (N2 + 1, N2 + 1500, 0, 1, 1000)
+    kw = dict(N2=N2, M=M, NT=nt, h=h, tao=tao, f0=f0, adaptive=True, compen=True, rec=rec)
+    pmig = build_problem(vmig, coef_table=table, **kw)
+    info = dict(info_box)
+    # optimiser alone on the same bins, for the comparison
+    sel = np.nonzero(info["err_used"] >= 0)[0]
+    r = (pmig.vmin + sel) * float(f32(tao)) / float(f32(h))
+    bb = 2.0 * 3.1415926535898 * float(f32(fmax)) * float(f32(tao)) / r
+    t1 = time.perf_counter()
+    copt = coeffs.ls_coefs(r, bb, M)
+    t_opt = time.perf_counter() - t1
+    err_opt = mlp.dispersion_error(copt, np.full(len(sel), M), r, bb)
+    err_net = info["err_net"][sel]
+    ptrue = build_problem(vtrue, coef_table=table, **kw)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    rng = np.random.default_rng(1240)
+    wn = rng.integers(1500, nx + 1, nshot)
+    xa = np.array([rng.integers(max(0, 2500 - w), min(1500, nx - w) + 1) for w in wn])
+    xs = xa + wn // 2
+    src_full = [pmig.src_flat(N2 + 1, N2 + int(x)) for x in xs]
+    seis = torch.zeros((nshot, pmig.nrec, nt), dtype=torch.float32, device="cuda")
+    tmp = torch.zeros_like(seis)
+    with Engine(ptrue, batch=min(nshot, 8), stream=sh) as e:
+        e.model(src_full, out=seis)
+    with Engine(pmig, batch=min(nshot, 8), stream=sh) as e:
+        e.model(src_full, out=tmp)
+    seis -= tmp
+    del tmp
+    p2, seis2 = pmig, seis
+    wsrc = [(N2 + 1) * (int(w) + 2 * N2) + N2 + int(x) - int(x0) for x, x0, w in zip(xs, xa, wn)]
+    eng = Engine(p2, batch=nshot, stream=sh, ring_precision=capi.RTM_RING_BF16)
+    tuned = eng.autotune(wsrc, xa, wn, nsteps=10)
+    kern = eng.kernel()
+    img = torch.zeros((nz, nx), dtype=torch.float32, device="cuda")
+    ill = torch.zeros_like(img)
+
+    def step():
+        eng.migrate_stack_windows(wsrc, xa, wn, seis2, 1e-4, nshot, True, image=img, illum=ill)
+
+    for _ in range(max(3, a.warmup)):
+        step()
+    torch.cuda.synchronize()
+    eng.launches(reset=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks("/tmp/bench_clocks_c5.csv") as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    NZ = nz + 2 * N2
+    cu = sum(nt * (2 * NZ * (int(w) + 2 * N2) + nz * int(w)) for w in wn)
+    used = info["err_used"][sel]
+    line = {"metric": METRIC, "value": cu / (ms / 1e3) / 1e9, "unit": METRIC, "n_gpus": 1,
+            "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "learned coefficients + full stack: 1201x4001 model, dx=dz=10 m, "
+                                   "%d shots with aperture windows of 1500-4001 columns, 1000 surface "
+                                   "receivers, %d steps, "
+                                   "M=%d MLP table (optimiser fallback above 1e-4), BF16 rings"
+                                   % (nshot, nt, M),
+                       "shots": nshot, "nt": nt, "mean_window": float(np.mean(wn)),
+                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split"][kern["fwd"]],
+                                     "bwd_kernel": ["tiled", "persistent", "tiled-split"][kern["bwd"]],
+                                     "shots_per_launch": kern["shots_per_launch"],
+                                     "tuning_gcells_per_s": tuned},
+                       "l2": "inputs larger than L2 (%.1f GB)" % (eng.device_bytes / 1e9)},
+            "coefficients": {"bins": int(len(sel)), "from_network": int(len(sel) - info["fallback"]),
+                             "tolerance": 1e-4, "max_dispersion_error_network": float(err_net.max()),
+                             "max_dispersion_error_optimiser": float(err_opt.max()),
+                             "max_dispersion_error_table": float(used.max()),
+                             "network_train_s": t_train, "network_train_loss": train_loss,
+                             "table_s": info["seconds"], "optimiser_alone_s": t_opt},
+            "clocks": clk.summary(0), "gpu_launches": eng.launches()}
+    print(json.dumps(line))
+    eng.close()
+
+
 def main():
     a = parse()
     cfg = Config(a)
@@ -361,6 +482,9 @@ def main():
         return
     if a.workload == "rvsp":
         run_rvsp(a, cfg)
+        return
+    if a.workload == "c5":
+        run_c5(a, cfg)
         return
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -397,7 +521,8 @@ def main():
     if a.kernel == "auto":
         tuned = eng.autotune(src, nsteps=20)
     else:
-        v = capi.RTM_KERNEL_TILED if a.kernel == "tiled" else capi.RTM_KERNEL_PERSISTENT
+        v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
+             "split": capi.RTM_KERNEL_SPLIT}[a.kernel]
         eng.set_kernel(v, v)
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
@@ -507,8 +632,8 @@ def main():
                 "steps": a.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(cfg.workload(), batch=batch,
-                               kernels={"fwd": ["tiled", "persistent"][kern["fwd"]],
-                                        "bwd": ["tiled", "persistent"][kern["bwd"]],
+                               kernels={"fwd": ["tiled", "persistent", "tiled-split"][kern["fwd"]],
+                                        "bwd": ["tiled", "persistent", "tiled-split"][kern["bwd"]],
                                         "shots_per_launch": kern["shots_per_launch"],
                                         "chosen_by": "autotuner" if tuned is not None else "flag",
                                         "tuning_gcells_per_s": tuned},

@@ -293,10 +293,12 @@ int rtm_ctx_launches(rtm_ctx *ctx, long *count, int reset);
 /* Stencil kernel form and shots per launch (no reference counterpart: the
  * reference launches one shot at a time).  RTM_KERNEL_TILED: one CTA per
  * 128 x 16 tile of every shot; RTM_KERNEL_PERSISTENT (default): a fixed grid
- * of resident CTAs walks the batch's tiles with a two-stage TMA pipeline.
+ * of resident CTAs walks the batch's tiles with a two-stage TMA pipeline;
+ * RTM_KERNEL_SPLIT: the tiled kernel with the two halves of a batch on two
+ * streams, so one half's pad launches overlap the other's stencil launches.
  * Set separately for the forward and the backward stencil; shots_per_launch
  * in 1..max_batch (0: max_batch). */
-enum { RTM_KERNEL_TILED = 0, RTM_KERNEL_PERSISTENT = 1 };
+enum { RTM_KERNEL_TILED = 0, RTM_KERNEL_PERSISTENT = 1, RTM_KERNEL_SPLIT = 2 };
 int rtm_ctx_set_kernel(rtm_ctx *ctx, int fwd_variant, int bwd_variant, int shots_per_launch);
 int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
                        int *shots_per_launch);

@@ -68,6 +68,8 @@ struct rtm_ctx {
     long ringsz = 0;        // cells per ring slot
     cudaStream_t st = nullptr;
     bool own_stream = false;  // created by the context (graphs cannot capture the legacy stream)
+    cudaStream_t st2 = nullptr;           // second half-batch stream (RTM_KERNEL_SPLIT)
+    cudaEvent_t evf[2] = {nullptr, nullptr};  // fork / join of the two streams
     std::vector<float> wav; // host wavelet table
     float vmax = 0.f;
     int nbins = 1;
@@ -139,6 +141,13 @@ int dalloc(rtm_ctx *c, T **p, size_t n)
 
 void free_all(rtm_ctx *c)
 {
+    if (c->st2) cudaStreamDestroy(c->st2);
+    c->st2 = nullptr;
+    for (cudaEvent_t &e : c->evf)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
     float *fl[] = {c->mvv, c->mvvs, c->v, c->r1, c->w, c->ctab, c->S[0], c->S[1], c->S[2], c->R[0], c->R[1], c->R[2],
@@ -185,7 +194,7 @@ int &pipe_grid()
 }
 
 template <int MMAX, bool AD, int MODE>
-int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb)
+int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb, cudaStream_t st)
 {
     const eng::ModelMaps &fv = c->windowed ? c->mmaps_s : c->mmaps;
     if (c->kv[MODE] == RTM_KERNEL_PERSISTENT) {
@@ -196,8 +205,8 @@ int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb)
     }
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
-    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, c->st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
-                                                                      c->imaps, a);
+    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
+                                                                   c->imaps, a);
     return RTM_OK;
 }
 
@@ -235,22 +244,22 @@ void init_step_attrs()
 }
 
 template <int MMAX>
-int launch_step_m(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb)
+int launch_step_m(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb, cudaStream_t st)
 {
     const bool ad = c->p.adaptive != 0;
     if (mode == eng::MODE_FWD)
-        return ad ? launch_step_t<MMAX, true, eng::MODE_FWD>(c, m, a, nb)
-                  : launch_step_t<MMAX, false, eng::MODE_FWD>(c, m, a, nb);
-    return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, m, a, nb)
-              : launch_step_t<MMAX, false, eng::MODE_BWD>(c, m, a, nb);
+        return ad ? launch_step_t<MMAX, true, eng::MODE_FWD>(c, m, a, nb, st)
+                  : launch_step_t<MMAX, false, eng::MODE_FWD>(c, m, a, nb, st);
+    return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, m, a, nb, st)
+              : launch_step_t<MMAX, false, eng::MODE_BWD>(c, m, a, nb, st);
 }
 
-int launch_step(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb)
+int launch_step(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb, cudaStream_t st)
 {
     switch (c->MM) {
-    case 4: return launch_step_m<4>(c, mode, m, a, nb);
-    case 8: return launch_step_m<8>(c, mode, m, a, nb);
-    case 12: return launch_step_m<12>(c, mode, m, a, nb);
+    case 4: return launch_step_m<4>(c, mode, m, a, nb, st);
+    case 8: return launch_step_m<8>(c, mode, m, a, nb, st);
+    case 12: return launch_step_m<12>(c, mode, m, a, nb, st);
     default: rtm_set_last_error("unsupported operator length"); return RTM_ERR_UNSUPPORTED;
     }
 }
@@ -310,6 +319,35 @@ void toc(rtm_ctx *c, int kind)
     else { c->ms_pad += ms; c->n_pad++; }
 }
 
+// Kernel form RTM_KERNEL_SPLIT: the two halves of a batch run their time
+// loops on two streams.  Their shots are independent, so the latency-bound
+// pad launches of one half overlap the other half's stencil launches (the
+// backward stencil leaves room for a pad CTA on every SM).
+struct Half {
+    int shot0, n;
+    cudaStream_t st;
+};
+
+int halves(rtm_ctx *c, int mode, int nb, Half h[2])
+{
+    if (c->kv[mode] == RTM_KERNEL_SPLIT && nb >= 2 && !c->timing && c->st2) {
+        h[0] = Half{0, nb / 2, c->st};
+        h[1] = Half{nb / 2, nb - nb / 2, c->st2};
+        cudaEventRecord(c->evf[0], c->st);
+        cudaStreamWaitEvent(c->st2, c->evf[0], 0);
+        return 2;
+    }
+    h[0] = Half{0, nb, c->st};
+    return 1;
+}
+
+void join(rtm_ctx *c, int nh)
+{
+    if (nh < 2) return;
+    cudaEventRecord(c->evf[1], c->st2);
+    cudaStreamWaitEvent(c->st, c->evf[1], 0);
+}
+
 // Forward run of nb shots (sources already in c->src).  rec_on: record the
 // receivers into c->rec (time-major [shot][NT][nrec]).
 int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
@@ -346,15 +384,14 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT) + (rec_on ? c->nrec : 0) +
                       (r16 ? c->ringsz : 0);
     const int kend = c->kstop ? std::min(c->kstop, NT) : NT;  // kstop-2 steps when tuning
+    Half hv[2];
+    const int nh = halves(c, eng::MODE_FWD, nb, hv);
     for (int k = 2; k < kend; ++k) {
         float *a0 = c->S[(k - 2) % 3], *a1 = c->S[(k - 1) % 3], *a2 = c->S[k % 3];
         sa.a0 = a0; sa.a2 = a2; sa.pre = c->pre;
         sa.wavelet = (k < c->p.NT2) ? c->wav[k - 1] : 0.0f;
-        tic(c);
         const StepMaps sm{&c->mapS[(k - 1) % 3], &c->mapS[(k - 1) % 3], &c->flatS[(k - 2) % 3],
                           &c->flatS[(k - 2) % 3]};
-        if (int rc = launch_step(c, eng::MODE_FWD, sm, sa, nb)) return rc;
-        toc(c, 0);
         pa.a0 = a0; pa.a1 = a1; pa.a2 = a2;
         pa.ring_mode = c->M > 0 ? 1 : 0;
         pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
@@ -366,10 +403,17 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         }
         pa.rec = rec_on ? c->rec + (long long)(k - 1) * c->nrec : nullptr;
         pa.rec_ss = rss;
-        tic(c);
-        eng::k_pad<<<dim3(cdiv(npad, 256), nb), 256, 0, c->st>>>(pa);
-        toc(c, 2);
+        for (int h = 0; h < nh; ++h) {
+            sa.shot0 = pa.shot0 = hv[h].shot0;
+            tic(c);
+            if (int rc = launch_step(c, eng::MODE_FWD, sm, sa, hv[h].n, hv[h].st)) return rc;
+            toc(c, 0);
+            tic(c);
+            eng::k_pad<<<dim3(cdiv(npad, 256), hv[h].n), 256, 0, hv[h].st>>>(pa);
+            toc(c, 2);
+        }
     }
+    join(c, nh);
     if (rec_on && c->nrec > 0)
         eng::k_record<<<dim3(cdiv(c->nrec, 128), nb), 128, 0, c->st>>>(
             c->S[(NT - 1) % 3], c->rec + (long long)(NT - 1) * c->nrec, ss, rss, c->P, c->p.rz0,
@@ -397,26 +441,32 @@ int enqueue_backward(rtm_ctx *c, int nb)
     eng::PadArgs pa = base_pad(c);
     const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT);
     const int kend = c->kstop ? std::max(NT - c->kstop, 0) : 0;  // kstop-2 steps when tuning
+    Half hv[2];
+    const int nh = halves(c, eng::MODE_BWD, nb, hv);
     for (int k = NT - 3; k >= kend; --k) {
         const int i2 = k % 3, i1 = (k + 1) % 3, i0 = (k + 2) % 3;
         sa.a0 = c->R[i0]; sa.a2 = c->R[i2]; sa.pre = c->pre;
         sa.s0 = c->S[i0]; sa.s2 = c->S[i2];
         sa.wavelet = (k < c->p.NT2) ? c->wav[k + 1] : 0.0f;
         sa.dinj = c->data + (long long)(k + 1) * c->nrec;
-        tic(c);
         const StepMaps sm{&c->mapR[i1], &c->mapS[i1], &c->flatR[i0], &c->flatS[i0]};
-        if (int rc = launch_step(c, eng::MODE_BWD, sm, sa, nb)) return rc;
-        toc(c, 1);
         pa.a0 = c->R[i0]; pa.a1 = c->R[i1]; pa.a2 = c->R[i2];
         pa.ring_mode = c->M > 0 ? 2 : 0;
         pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
         pa.slot = k;
         pa.s2 = c->S[i2];
         pa.rec = nullptr;
-        tic(c);
-        eng::k_pad<<<dim3(cdiv(npad, 256), nb), 256, 0, c->st>>>(pa);
-        toc(c, 2);
+        for (int h = 0; h < nh; ++h) {
+            sa.shot0 = pa.shot0 = hv[h].shot0;
+            tic(c);
+            if (int rc = launch_step(c, eng::MODE_BWD, sm, sa, hv[h].n, hv[h].st)) return rc;
+            toc(c, 1);
+            tic(c);
+            eng::k_pad<<<dim3(cdiv(npad, 256), hv[h].n), 256, 0, hv[h].st>>>(pa);
+            toc(c, 2);
+        }
     }
+    join(c, nh);
     RTM_LAUNCH_CHECK();
     return RTM_OK;
 }
@@ -648,6 +698,14 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     } else {
         c->own_stream = true;
     }
+    if (cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->evf[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess) {
+        rtm_set_last_error("cudaStreamCreate failed");
+        free_all(c);
+        delete c;
+        return RTM_ERR_CUDA;
+    }
     if (p->adaptive) {
         c->nbins = p->nbins;
         tab.assign((size_t)(c->MM + 1) * c->nbins, 0.0f);
@@ -871,7 +929,7 @@ int rtm_ctx_timing(const rtm_ctx *c, double ms[3], long n[3])
 
 int rtm_ctx_set_kernel(rtm_ctx *c, int fwd_variant, int bwd_variant, int shots_per_launch)
 {
-    auto ok = [](int v) { return v == RTM_KERNEL_TILED || v == RTM_KERNEL_PERSISTENT; };
+    auto ok = [](int v) { return v == RTM_KERNEL_TILED || v == RTM_KERNEL_PERSISTENT || v == RTM_KERNEL_SPLIT; };
     if (!c || !ok(fwd_variant) || !ok(bwd_variant) || shots_per_launch < 0 || shots_per_launch > c->B)
         return RTM_ERR_ARG;
     if (fwd_variant != c->kv[0] || bwd_variant != c->kv[1]) {
@@ -913,8 +971,9 @@ int rtm_ctx_autotune(rtm_ctx *c, int nshot, const int *src_cells, const int *win
         double cells = 0;  // cell updates of one forward + one backward step of the batch
         for (int i = 0; i < nb; ++i)
             cells += (double)c->NZ * c->hnx[i] + (double)c->nz * (c->hnx[i] - 2 * c->N2);
-        double fwd_ms[2], bwd_ms[2];
-        for (int v = 0; v < 2 && rc == RTM_OK; ++v) {
+        constexpr int NV = 3;  // tiled, persistent, tiled in two stream halves
+        double fwd_ms[NV], bwd_ms[NV];
+        for (int v = 0; v < NV && rc == RTM_OK; ++v) {
             c->kv[0] = c->kv[1] = v;
             c->kstop = 2 + 1;  // warm-up: one step of each phase
             if ((rc = enqueue_forward(c, nb, false)) || (rc = enqueue_backward(c, nb))) break;
@@ -932,7 +991,11 @@ int rtm_ctx_autotune(rtm_ctx *c, int nshot, const int *src_cells, const int *win
             bwd_ms[v] = b;
         }
         if (rc) break;
-        const int vf = fwd_ms[1] < fwd_ms[0] ? 1 : 0, vb = bwd_ms[1] < bwd_ms[0] ? 1 : 0;
+        int vf = 0, vb = 0;
+        for (int v = 1; v < NV; ++v) {
+            if (fwd_ms[v] < fwd_ms[vf]) vf = v;
+            if (bwd_ms[v] < bwd_ms[vb]) vb = v;
+        }
         const double rate = cells * nsteps / ((fwd_ms[vf] + bwd_ms[vb]) * 1e-3) / 1e9;
         if (rate > best) {
             best = rate;

@@ -114,6 +114,7 @@ struct StepArgs {
     // shot's grid; vshot = 1 when every shot has its own model copy
     const int *nxs, *rx0s;
     int vshot;
+    int shot0;                 // first shot of this launch (blockIdx.z + shot0)
 };
 
 __device__ __forceinline__ int mirror_i(int i, int n)
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     extern __shared__ __align__(128) float smem[];
     const Stage<MMAX, MODE> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
-    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z;
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
     const int NX = a.nxs[shot];
     if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
 
@@ -580,6 +581,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
 
 struct PadArgs {
     int NZ, P, N2, M;
+    int shot0;                // first shot of this launch (blockIdx.y + shot0)
     long long ss;
     long nabc;                // pad cells of the widest grid (threads per shot)
     const int *nxs, *rx0s;    // per-shot padded width and receiver start column
@@ -716,7 +718,7 @@ __device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long
 __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
 {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int shot = blockIdx.y;
+    const int shot = blockIdx.y + a.shot0;
     const long long so = (long long)shot * a.ss;
     const int NX = a.nxs[shot];
     const long npadt = (a.nabc + PAD_CPT - 1) / PAD_CPT;  // threads of the pad cells

@@ -12,7 +12,7 @@ from test_gpu_windows import window_problem
 from util import interior, rel_l2, small_problem
 
 pytestmark = pytest.mark.gpu
-TILED, PERSISTENT = capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_PERSISTENT
+TILED, PERSISTENT, SPLIT = capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_PERSISTENT, capi.RTM_KERNEL_SPLIT
 
 
 def _seis(p, n, seed):
@@ -27,7 +27,8 @@ def test_forms_bit_identical(product_lib, cuda_ok, adaptive):
     seis = _seis(p, len(srcs), 3)
     out = {}
     with Engine(p, batch=5) as e:
-        for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (TILED, PERSISTENT)):
+        for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (TILED, PERSISTENT), (SPLIT, SPLIT),
+                         (PERSISTENT, SPLIT)):
             e.set_kernel(fwd, bwd)
             assert e.kernel() == {"fwd": fwd, "bwd": bwd, "shots_per_launch": 5}
             out[(fwd, bwd)] = e.migrate(srcs, seis)
@@ -47,11 +48,12 @@ def test_forms_bit_identical_uneven_windows(product_lib, cuda_ok):
     seis = _seis(p, len(wins), 4)
     res = []
     with Engine(p, batch=5) as e:
-        for v in (TILED, PERSISTENT):
+        for v in (TILED, PERSISTENT, SPLIT):
             e.set_kernel(v)
             res.append(e.migrate_stack_windows(srcs, [w[0] for w in wins], [w[1] for w in wins],
                                                seis, 1e-4, len(wins), True))
-    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    for r in res[1:]:
+        assert np.array_equal(res[0][0], r[0]) and np.array_equal(res[0][1], r[1])
 
 
 def test_shots_per_launch(product_lib, cuda_ok):
@@ -75,7 +77,7 @@ def test_autotune_then_oracle(product_lib, cuda_ok):
         rate = e.autotune(srcs, nsteps=10)
         k = e.kernel()
         assert rate > 0
-        assert k["fwd"] in (TILED, PERSISTENT) and k["bwd"] in (TILED, PERSISTENT)
+        assert k["fwd"] in (TILED, PERSISTENT, SPLIT) and k["bwd"] in (TILED, PERSISTENT, SPLIT)
         assert k["shots_per_launch"] in (8, 4)
         g1, g2 = e.migrate(srcs, seis)
     for i in (0, 5, 7):
@@ -83,3 +85,48 @@ def test_autotune_then_oracle(product_lib, cuda_ok):
         o1, o2 = orc.migrate(q, seis[i])
         assert rel_l2(interior(p, g1[i]), interior(p, o1)) < 1e-4
         assert rel_l2(interior(p, g2[i]), interior(p, o2)) < 1e-4
+
+
+def test_few_and_many_bins_per_tile(product_lib, cuda_ok):
+    """A model whose first tile column has few velocity bins and whose others
+    have nearly a bin per cell (1100 bins, scattered coefficient gathers):
+    both kernel forms bit-identical and against the oracle."""
+    from rtm_gpu_gb300.problem import build_problem
+    from util import oracle_table
+    N2, nz, nx = 8, 40, 300
+    rng = np.random.default_rng(21)
+    vin = np.full((nz, nx), 2000.0, np.float32)
+    vin += (np.arange(nz)[:, None] * 2.0).astype(np.float32)          # ~80 bins down the tile
+    vin[:, 150:] = rng.uniform(1500.0, 2600.0, (nz, nx - 150)).astype(np.float32)  # ~1100 bins
+    p = build_problem(vin, N2=N2, M=4, NT=120, h=10.0, tao=0.001, f0=25.0, adaptive=True, compen=True,
+                      rec=(N2 + 1, N2, 0, 3, 100), coef_table=oracle_table(4, 0.001, 10.0, 50.0))
+    srcs = [p.src_flat(N2 + 2, N2 + x) for x in (40, 220)]
+    seis = _seis(p, len(srcs), 9)
+    with Engine(p, batch=2) as e:
+        res = {}
+        for v in (TILED, PERSISTENT):
+            e.set_kernel(v)
+            res[v] = e.migrate(srcs, seis)
+    assert np.array_equal(res[TILED][0], res[PERSISTENT][0])
+    for i, s in enumerate(srcs):
+        q = p.with_source(s // p.NX, s % p.NX)
+        o1, o2 = orc.migrate(q, seis[i])
+        assert rel_l2(interior(p, res[TILED][0][i]), interior(p, o1)) < 1e-4
+        assert rel_l2(interior(p, res[TILED][1][i]), interior(p, o2)) < 1e-4
+
+
+def test_split_modelling_and_fp16_rings(product_lib, cuda_ok):
+    """Forward modelling (receiver recording in the pad launches) and FP16
+    rings with per-step scaling under the two-stream split: identical to one
+    stream."""
+    p = small_problem(nx=120, nz=40, NT=100)
+    srcs = [p.src_flat(p.N2 + 1, p.N2 + x) for x in (5, 30, 60, 90, 110)]
+    seis = _seis(p, len(srcs), 11)
+    out = {}
+    with Engine(p, batch=5, ring_precision=capi.RTM_RING_F16) as e:
+        for v in (TILED, SPLIT):
+            e.set_kernel(v)
+            out[v] = (e.model(srcs), e.migrate(srcs, seis))
+    assert np.array_equal(out[TILED][0], out[SPLIT][0])
+    assert np.array_equal(out[TILED][1][0], out[SPLIT][1][0])
+    assert np.array_equal(out[TILED][1][1], out[SPLIT][1][1])
