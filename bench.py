@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--cpu-sample-nt", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split", "x2"],
                     help="stencil kernel form (auto: the autotuner picks it and shots per launch)")
     ap.add_argument("--workload", default="multishot", choices=["multishot", "rvsp", "c5"],
                     help="rvsp: batched uneven aperture windows, well receivers, autotuned; "
@@ -291,8 +291,8 @@ def run_rvsp(a, cfg):
         tuned = eng.autotune(wsrc, xa, wn, nsteps=20)
     else:
         v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
-             "split": capi.RTM_KERNEL_SPLIT}[a.kernel]
-        eng.set_kernel(v, v)
+             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2}[a.kernel]
+        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v == capi.RTM_KERNEL_X2 else v)
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
@@ -337,8 +337,8 @@ def run_rvsp(a, cfg):
                                    % (cfg.nz, cfg.nx, nshot, rec[4], 50 + rec[4] - 1, cfg.NT,
                                       cfg.M, cfg.coef, cfg.ring.upper()),
                        "shots": nshot, "mean_window": float(np.mean(wn)), "batch": batch,
-                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split"][kern["fwd"]],
-                                     "bwd_kernel": ["tiled", "persistent", "tiled-split"][kern["bwd"]],
+                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["fwd"]],
+                                     "bwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["bwd"]],
                                      "shots_per_launch": kern["shots_per_launch"],
                                      "tuning_gcells_per_s": tuned},
                        "l2": "inputs larger than L2 (%.1f GB of wavefields and rings)"
@@ -456,8 +456,8 @@ def run_c5(a, cfg):
                                    "M=%d MLP table (optimiser fallback above 1e-4), BF16 rings"
                                    % (nshot, nt, M),
                        "shots": nshot, "nt": nt, "mean_window": float(np.mean(wn)),
-                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split"][kern["fwd"]],
-                                     "bwd_kernel": ["tiled", "persistent", "tiled-split"][kern["bwd"]],
+                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["fwd"]],
+                                     "bwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["bwd"]],
                                      "shots_per_launch": kern["shots_per_launch"],
                                      "tuning_gcells_per_s": tuned},
                        "l2": "inputs larger than L2 (%.1f GB)" % (eng.device_bytes / 1e9)},
@@ -498,6 +498,13 @@ def main():
 
     ptrue, pmig, shots = build_problems(cfg)
     nshot = cfg.nshot
+    if world > 1:
+        # sharded survey: nshot shots per rank out of nshot * world along the
+        # surface (weak scaling), stacks combined by one all-reduce per step
+        from rtm_gpu_gb300 import synth
+        from rtm_gpu_gb300.shard import shard_shots
+        survey = synth.surface_shots(cfg.nx, nshot * world, cfg.N2)
+        shots = [survey[i] for i in shard_shots(len(survey), rank, world)]
     batch = a.batch or nshot
     src = [pmig.src_flat(z, x) for z, x in shots]
     stream = torch.cuda.Stream()
@@ -522,14 +529,25 @@ def main():
         tuned = eng.autotune(src, nsteps=20)
     else:
         v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
-             "split": capi.RTM_KERNEL_SPLIT}[a.kernel]
-        eng.set_kernel(v, v)
+             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2}[a.kernel]
+        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v == capi.RTM_KERNEL_X2 else v)
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
 
+    s1 = torch.zeros((2, pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
+
     def step_dev():
-        eng.migrate_stack(src, seis, cfg.whitecoe, nshot, True, image=img, illum=ill)
+        if not dist:
+            eng.migrate_stack(src, seis, cfg.whitecoe, nshot, True, image=img, illum=ill)
+            return
+        # the rank's sums of the per-shot images (no normalisation), summed
+        # over ranks, then kernel.cu:1042-1059's normalisation
+        eng.migrate_stack(src, seis, cfg.whitecoe, 1, False, image=s1[0], illum=s1[1])
+        dist.all_reduce(s1, op=dist.ReduceOp.SUM)
+        ntot = float(nshot * world)
+        torch.div(s1[1], ntot, out=ill)
+        torch.div(torch.div(s1[0], ntot), ill, out=img)
 
     for _ in range(warm):
         step_dev()
@@ -632,8 +650,8 @@ def main():
                 "steps": a.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(cfg.workload(), batch=batch,
-                               kernels={"fwd": ["tiled", "persistent", "tiled-split"][kern["fwd"]],
-                                        "bwd": ["tiled", "persistent", "tiled-split"][kern["bwd"]],
+                               kernels={"fwd": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["fwd"]],
+                                        "bwd": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["bwd"]],
                                         "shots_per_launch": kern["shots_per_launch"],
                                         "chosen_by": "autotuner" if tuned is not None else "flag",
                                         "tuning_gcells_per_s": tuned},

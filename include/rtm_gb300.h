@@ -295,10 +295,11 @@ int rtm_ctx_launches(rtm_ctx *ctx, long *count, int reset);
  * 128 x 16 tile of every shot; RTM_KERNEL_PERSISTENT (default): a fixed grid
  * of resident CTAs walks the batch's tiles with a two-stage TMA pipeline;
  * RTM_KERNEL_SPLIT: the tiled kernel with the two halves of a batch on two
- * streams, so one half's pad launches overlap the other's stencil launches.
+ * streams, so one half's pad launches overlap the other's stencil launches;
+ * RTM_KERNEL_X2 (forward only): the tiled kernel with two columns per lane.
  * Set separately for the forward and the backward stencil; shots_per_launch
  * in 1..max_batch (0: max_batch). */
-enum { RTM_KERNEL_TILED = 0, RTM_KERNEL_PERSISTENT = 1, RTM_KERNEL_SPLIT = 2 };
+enum { RTM_KERNEL_TILED = 0, RTM_KERNEL_PERSISTENT = 1, RTM_KERNEL_SPLIT = 2, RTM_KERNEL_X2 = 3 };
 int rtm_ctx_set_kernel(rtm_ctx *ctx, int fwd_variant, int bwd_variant, int shots_per_launch);
 int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
                        int *shots_per_launch);
@@ -310,6 +311,12 @@ int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
  * afterwards. */
 int rtm_ctx_autotune(rtm_ctx *ctx, int nshot, const int *src_cells, const int *win_x0,
                      const int *win_nx, int nsteps, double *gcells_per_s);
+
+/* Self-test of the device-side bounded waits (no reference counterpart):
+ * a kernel waits `polls` (1..2^20) times on an mbarrier that nothing
+ * completes, gives up, and the device error word is read back into *code
+ * (RTM_DEVERR_TMA_TIMEOUT = 1 expected); the context stays usable. */
+int rtm_selftest_wait_timeout(unsigned polls, unsigned int *code);
 
 /* ======================================================================
  * 5. The reference's file flow.

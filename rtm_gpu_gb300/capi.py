@@ -19,7 +19,7 @@ RTM_OK = 0
 RTM_DEVICE_PTRS = 1
 RTM_NO_GRAPH = 2
 RTM_RING_F32, RTM_RING_BF16, RTM_RING_F16 = 0, 1, 2
-RTM_KERNEL_TILED, RTM_KERNEL_PERSISTENT, RTM_KERNEL_SPLIT = 0, 1, 2
+RTM_KERNEL_TILED, RTM_KERNEL_PERSISTENT, RTM_KERNEL_SPLIT, RTM_KERNEL_X2 = 0, 1, 2, 3
 
 vp = C.c_void_p
 fp = C.POINTER(C.c_float)
@@ -101,6 +101,7 @@ def lib():
         L.rtm_ctx_get_kernel.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.rtm_ctx_autotune.argtypes = [vp, I, ip, ip, ip, I, C.POINTER(C.c_double)]
         L.rtm_resample.argtypes = [fp, I, I, C.c_float, fp, I, C.c_float, I]
+        L.rtm_selftest_wait_timeout.argtypes = [C.c_uint, C.POINTER(C.c_uint)]
         L.rtm_run_config.argtypes = [C.c_char_p, I]
         L.rtm_depth_to_time.argtypes = [fp, fp, I, I, C.c_float, C.c_float, fp, C.c_long,
                                         C.POINTER(C.c_int), I]

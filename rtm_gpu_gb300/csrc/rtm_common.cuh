@@ -75,9 +75,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
 // Waits for phase `parity` of the barrier, at most RTM_SPIN_LIMIT polls.
 // Returns false (and ORs RTM_DEVERR_TMA_TIMEOUT into *err) when the limit is
 // hit, so a lost copy ends the kernel with an error instead of a hang.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, unsigned *err)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, unsigned *err,
+                                                  unsigned limit = RTM_SPIN_LIMIT)
 {
-    for (unsigned it = 0; it < RTM_SPIN_LIMIT; ++it)
+    for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     atomicOr(err, RTM_DEVERR_TMA_TIMEOUT);
     return false;

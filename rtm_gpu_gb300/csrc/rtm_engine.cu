@@ -205,6 +205,11 @@ int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb,
     }
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
+    if (MODE == eng::MODE_FWD && c->kv[MODE] == RTM_KERNEL_X2) {
+        eng::k_step_x2<MMAX, AD><<<grid, eng::X2_THREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
+                                                                     c->imaps, a);
+        return RTM_OK;
+    }
     eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
                                                                    c->imaps, a);
     return RTM_OK;
@@ -215,6 +220,8 @@ void set_attr_t()
 {
     const int smem = (int)eng::Smem<MMAX, MODE>::BYTES;
     cudaFuncSetAttribute(eng::k_step<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (MODE == eng::MODE_FWD)
+        cudaFuncSetAttribute(eng::k_step_x2<MMAX, AD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     const int psmem = (int)eng::PipeSmem<MMAX, MODE>::BYTES;
     cudaFuncSetAttribute(eng::k_step_pipe<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem);
     int dev = 0, sms = 0, occ = 0;
@@ -629,6 +636,31 @@ int copy_grid_out(rtm_ctx *c, const float *dsrc, float *dst, int nb, bool dev)
 
 extern "C" {
 
+// Self-test of the bounded waits: one CTA waits on an mbarrier that nothing
+// completes, for `polls` polls; every thread gives up, records the timeout in
+// the device error word and returns.
+__global__ void k_wait_selftest(unsigned polls)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    mbar_wait_bounded(&bar, 0, &g_rtm_dev_error, polls);
+}
+
+int rtm_selftest_wait_timeout(unsigned polls, unsigned int *code)
+{
+    if (!code || polls < 1 || polls > (1u << 20)) return RTM_ERR_ARG;
+    unsigned z = 0;
+    RTM_CUDA_TRY(cudaMemcpyToSymbol(g_rtm_dev_error, &z, sizeof(z)));
+    k_wait_selftest<<<1, 64>>>(polls);
+    RTM_CUDA_TRY(cudaGetLastError());
+    RTM_CUDA_TRY(cudaDeviceSynchronize());
+    return rtm_device_error(code);
+}
+
 int rtm_device_error(unsigned int *code)
 {
     unsigned v = 0, z = 0;
@@ -930,7 +962,8 @@ int rtm_ctx_timing(const rtm_ctx *c, double ms[3], long n[3])
 int rtm_ctx_set_kernel(rtm_ctx *c, int fwd_variant, int bwd_variant, int shots_per_launch)
 {
     auto ok = [](int v) { return v == RTM_KERNEL_TILED || v == RTM_KERNEL_PERSISTENT || v == RTM_KERNEL_SPLIT; };
-    if (!c || !ok(fwd_variant) || !ok(bwd_variant) || shots_per_launch < 0 || shots_per_launch > c->B)
+    if (!c || !(ok(fwd_variant) || fwd_variant == RTM_KERNEL_X2) || !ok(bwd_variant) || shots_per_launch < 0 ||
+        shots_per_launch > c->B)
         return RTM_ERR_ARG;
     if (fwd_variant != c->kv[0] || bwd_variant != c->kv[1]) {
         // captured graphs embed the old kernels
@@ -971,10 +1004,13 @@ int rtm_ctx_autotune(rtm_ctx *c, int nshot, const int *src_cells, const int *win
         double cells = 0;  // cell updates of one forward + one backward step of the batch
         for (int i = 0; i < nb; ++i)
             cells += (double)c->NZ * c->hnx[i] + (double)c->nz * (c->hnx[i] - 2 * c->N2);
-        constexpr int NV = 3;  // tiled, persistent, tiled in two stream halves
+        // tiled, persistent, tiled in two stream halves, two columns per
+        // lane (forward only: the backward form is timed as tiled there)
+        constexpr int NV = 4;
         double fwd_ms[NV], bwd_ms[NV];
         for (int v = 0; v < NV && rc == RTM_OK; ++v) {
-            c->kv[0] = c->kv[1] = v;
+            c->kv[0] = v;
+            c->kv[1] = v == RTM_KERNEL_X2 ? RTM_KERNEL_TILED : v;
             c->kstop = 2 + 1;  // warm-up: one step of each phase
             if ((rc = enqueue_forward(c, nb, false)) || (rc = enqueue_backward(c, nb))) break;
             c->kstop = 2 + nsteps;
@@ -994,7 +1030,7 @@ int rtm_ctx_autotune(rtm_ctx *c, int nshot, const int *src_cells, const int *win
         int vf = 0, vb = 0;
         for (int v = 1; v < NV; ++v) {
             if (fwd_ms[v] < fwd_ms[vf]) vf = v;
-            if (bwd_ms[v] < bwd_ms[vb]) vb = v;
+            if (v != RTM_KERNEL_X2 && bwd_ms[v] < bwd_ms[vb]) vb = v;
         }
         const double rate = cells * nsteps / ((fwd_ms[vf] + bwd_ms[vb]) * 1e-3) / 1e9;
         if (rate > best) {

@@ -125,7 +125,7 @@ __device__ __forceinline__ int mirror_i(int i, int n)
 // Mirror the out-of-grid halo of a staged box (the reference reflects
 // neighbour indices at the array edges, kernel.cu:65-68).  Only the tile's
 // own rows need x-halo values and only its own columns need z-halo values.
-template <int MMAX>
+template <int MMAX, int NT = NTHREADS>
 __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int NZ)
 {
     using S = Shape<MMAX>;
@@ -133,7 +133,7 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
     // x reflection on the tile's in-grid rows, z reflection on its in-grid
     // columns: the written and the read cells of the two passes never overlap.
     if (x0 == 0 || x0 + TX + S::XH > NX) {
-        for (int idx = threadIdx.x; idx < TZ * S::BW; idx += NTHREADS) {
+        for (int idx = threadIdx.x; idx < TZ * S::BW; idx += NT) {
             const int r = S::ZH + idx / S::BW, c = idx % S::BW;
             const int gx = gx0 + c, gz = gz0 + r;
             if ((gx >= 0 && gx < NX) || gz >= NZ) continue;
@@ -142,7 +142,7 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
         }
     }
     if (z0 == 0 || z0 + TZ + S::ZH > NZ) {
-        for (int idx = threadIdx.x; idx < S::BH * TX; idx += NTHREADS) {
+        for (int idx = threadIdx.x; idx < S::BH * TX; idx += NT) {
             const int r = idx / TX, c = S::XH + idx % TX;
             const int gz = gz0 + r, gx = gx0 + c;
             if ((gz >= 0 && gz < NZ) || gx >= NX) continue;
@@ -483,6 +483,135 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         return;
     }
     compute_tile<MMAX, ADAPT, MODE, PF>(a, st, cc, x0, z0, shot, NX);
+}
+
+// Forward step with two columns per lane (kernel form RTM_KERNEL_X2): the
+// same 128 x 16 tile and staging as k_step with 4 warps (2 across, 2 down);
+// each lane owns two adjacent columns, reads their z-queue entries and their
+// 2M+2 x-neighbours as 8-byte shared loads, and computes both cells with
+// k_step's operation order (bit-identical results).
+constexpr int X2_THREADS = 128;
+
+template <int MMAX, bool ADAPT>
+__device__ __forceinline__ float lap_regs(const float *q, int C, const float *xv, int o, const float *cf,
+                                          float k0, float hzx2_1)
+{
+    // xv[o + j] is the row's value at column (cell - MMAX + j)
+    float w1 = k0 * cf[0] * q[C];
+#pragma unroll
+    for (int l = 1; l <= MMAX; ++l) {
+        const float xs = (q[C - l] + q[C + l]) * hzx2_1 + xv[o + MMAX - l];
+        w1 = fmaf(cf[l], xs + xv[o + MMAX + l], w1);
+    }
+    return w1;
+}
+
+template <int MMAX, bool ADAPT>
+__global__ void __launch_bounds__(X2_THREADS, 4)
+    k_step_x2(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
+              const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
+              const __grid_constant__ ModelMaps mod, const __grid_constant__ ImgMaps img, const StepArgs a)
+{
+    using S = Shape<MMAX>;
+    constexpr int QN = 2 * MMAX + 1;
+    constexpr int NXV = 2 * MMAX + 2;  // x values covering both columns' stencils
+    extern __shared__ __align__(128) float smem[];
+    const Stage<MMAX, MODE_FWD> st(smem);
+    uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE_FWD>());
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
+    const int NX = a.nxs[shot];
+    if (x0 >= NX) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        issue_tile<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot,
+                                          a.vshot, false);
+    float cc[MMAX + 1];
+#pragma unroll
+    for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
+    const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
+    if (ok) patch_halo<MMAX, X2_THREADS>(st.tA, x0, z0, NX, a.NZ);
+    if (!__syncthreads_and(ok)) {
+        mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
+        return;
+    }
+    const float *tA = st.tA, *fA0 = st.fA0, *fV = st.fV;
+    const int *fB = st.fB;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wx = warp & 1, wz = warp >> 1;
+    const int c0 = wx * 64 + 2 * lane;        // first of the lane's two columns in the tile
+    const int gx = x0 + c0;
+    const int cx = S::XH + c0;                // its column in the halo box (even)
+    const int zw = z0 + wz * RW;
+    const int rbase = wz * RW;
+    const int fr = wz * RW * TX + c0;
+    const int src = a.src[shot];
+    const int sx = src % NX;
+    const int src_row0 = (sx == gx) ? src / NX - zw : -1;
+    const int src_row1 = (sx == gx + 1) ? src / NX - zw : -1;
+    const int N2 = a.N2, NZ = a.NZ;
+    const long long g0 = (long long)shot * a.ss + (long)zw * a.P + gx;
+    float qa[QN + 1], qb[QN + 1];  // z-queues of the two columns
+#pragma unroll
+    for (int j = 0; j < QN - 1; ++j) {
+        const float2 v = *reinterpret_cast<const float2 *>(tA + (rbase + j) * S::BW + cx);
+        qa[j] = v.x;
+        qb[j] = v.y;
+    }
+#pragma unroll
+    for (int i = 0; i < RW; i += 2) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float2 v = *reinterpret_cast<const float2 *>(tA + (rbase + i + QN - 1 + h) * S::BW + cx);
+            qa[QN - 1 + h] = v.x;
+            qb[QN - 1 + h] = v.y;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int z = zw + i + h;
+            if (z >= NZ) continue;
+            const int t = fr + (i + h) * TX;
+            const float *row = tA + (rbase + i + h + MMAX) * S::BW + cx - MMAX;  // even offset
+            float xv[NXV];
+#pragma unroll
+            for (int j = 0; j < NXV; j += 2) {
+                const float2 v = *reinterpret_cast<const float2 *>(row + j);
+                xv[j] = v.x;
+                xv[j + 1] = v.y;
+            }
+            float cfa[MMAX + 1], cfb[MMAX + 1];
+            const int2 bins = ADAPT ? *reinterpret_cast<const int2 *>(fB + t) : make_int2(0, 0);
+            load_coefs<MMAX, ADAPT>(a, bins.x, cc, cfa);
+            load_coefs<MMAX, ADAPT>(a, bins.y, cc, cfb);
+            const float2 vv = *reinterpret_cast<const float2 *>(fV + t);
+            const float2 u0 = *reinterpret_cast<const float2 *>(fA0 + t);
+            const float wa = lap_regs<MMAX, ADAPT>(qa, MMAX + h, xv, 0, cfa, a.k0, a.hzx2_1);
+            const float wb = lap_regs<MMAX, ADAPT>(qb, MMAX + h, xv, 1, cfb, a.k0, a.hzx2_1);
+            float va = fmaf(vv.x, wa, 2.0f * qa[MMAX + h] - u0.x);
+            float vb = fmaf(vv.y, wb, 2.0f * qb[MMAX + h] - u0.y);
+            if (i + h == src_row0) va += a.wavelet;
+            if (i + h == src_row1) vb += a.wavelet;
+            const bool zin = z >= N2 && z < NZ - N2, zring = z == N2 || z == NZ - 1 - N2;
+            const long long g = g0 + (long)(i + h) * a.P;
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const int x = gx + c;
+                if (x >= NX) continue;
+                const float val = c ? vb : va;
+                const bool interior = zin && x >= N2 && x < NX - N2;
+                if (interior) a.a2[g + c] = val;
+                if (!interior || x == N2 || x == NX - 1 - N2 || zring) a.pre[g + c] = val;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < QN - 1; ++j) {
+            qa[j] = qa[j + 2];
+            qb[j] = qb[j + 2];
+        }
+    }
 }
 
 // Persistent form of k_step: a fixed grid of CTAs walks the batch's tiles

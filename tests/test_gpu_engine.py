@@ -109,3 +109,23 @@ def test_migrate_stack_matches_oracle(product_lib, cuda_ok, vhi):
     assert rel_l2(gd, np.stack(downs)) < TOL
     assert rel_l2(ill, ill_o) < TOL
     assert rel_l2(img, img_o) < 10 * TOL
+
+
+def test_bounded_wait_gives_up_and_context_survives(product_lib, cuda_ok):
+    """A wait that nothing completes ends with the timeout flag in the device
+    error word (no hang, no trap); the next migration still runs and matches
+    the oracle."""
+    import ctypes as C
+    from rtm_gpu_gb300 import capi
+    code = C.c_uint(0)
+    capi.check(capi.lib().rtm_selftest_wait_timeout(2000, C.byref(code)), "selftest")
+    assert code.value == 1
+    code2 = C.c_uint(7)
+    capi.check(capi.lib().rtm_device_error(C.byref(code2)), "device_error")
+    assert code2.value == 0  # read and cleared
+    p = small_problem()
+    seis = _seis(p)
+    o1, o2 = orc.migrate(p, seis)
+    with Engine(p, batch=1) as e:
+        g1, g2 = e.migrate([p.src_flat()], seis[None])
+    assert rel_l2(interior(p, g1[0]), interior(p, o1)) < TOL

@@ -12,7 +12,8 @@ from test_gpu_windows import window_problem
 from util import interior, rel_l2, small_problem
 
 pytestmark = pytest.mark.gpu
-TILED, PERSISTENT, SPLIT = capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_PERSISTENT, capi.RTM_KERNEL_SPLIT
+TILED, PERSISTENT, SPLIT, X2 = (capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_PERSISTENT, capi.RTM_KERNEL_SPLIT,
+                                capi.RTM_KERNEL_X2)
 
 
 def _seis(p, n, seed):
@@ -28,7 +29,7 @@ def test_forms_bit_identical(product_lib, cuda_ok, adaptive):
     out = {}
     with Engine(p, batch=5) as e:
         for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (TILED, PERSISTENT), (SPLIT, SPLIT),
-                         (PERSISTENT, SPLIT)):
+                         (PERSISTENT, SPLIT), (X2, TILED)):
             e.set_kernel(fwd, bwd)
             assert e.kernel() == {"fwd": fwd, "bwd": bwd, "shots_per_launch": 5}
             out[(fwd, bwd)] = e.migrate(srcs, seis)
@@ -48,8 +49,8 @@ def test_forms_bit_identical_uneven_windows(product_lib, cuda_ok):
     seis = _seis(p, len(wins), 4)
     res = []
     with Engine(p, batch=5) as e:
-        for v in (TILED, PERSISTENT, SPLIT):
-            e.set_kernel(v)
+        for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (SPLIT, SPLIT), (X2, TILED)):
+            e.set_kernel(fwd, bwd)
             res.append(e.migrate_stack_windows(srcs, [w[0] for w in wins], [w[1] for w in wins],
                                                seis, 1e-4, len(wins), True))
     for r in res[1:]:
@@ -77,7 +78,7 @@ def test_autotune_then_oracle(product_lib, cuda_ok):
         rate = e.autotune(srcs, nsteps=10)
         k = e.kernel()
         assert rate > 0
-        assert k["fwd"] in (TILED, PERSISTENT, SPLIT) and k["bwd"] in (TILED, PERSISTENT, SPLIT)
+        assert k["fwd"] in (TILED, PERSISTENT, SPLIT, X2) and k["bwd"] in (TILED, PERSISTENT, SPLIT)
         assert k["shots_per_launch"] in (8, 4)
         g1, g2 = e.migrate(srcs, seis)
     for i in (0, 5, 7):
@@ -104,10 +105,11 @@ def test_few_and_many_bins_per_tile(product_lib, cuda_ok):
     seis = _seis(p, len(srcs), 9)
     with Engine(p, batch=2) as e:
         res = {}
-        for v in (TILED, PERSISTENT):
-            e.set_kernel(v)
+        for v in (TILED, PERSISTENT, X2):
+            e.set_kernel(v, TILED if v == X2 else v)
             res[v] = e.migrate(srcs, seis)
     assert np.array_equal(res[TILED][0], res[PERSISTENT][0])
+    assert np.array_equal(res[TILED][0], res[X2][0])
     for i, s in enumerate(srcs):
         q = p.with_source(s // p.NX, s % p.NX)
         o1, o2 = orc.migrate(q, seis[i])
