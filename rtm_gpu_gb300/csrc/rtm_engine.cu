@@ -283,6 +283,8 @@ eng::StepArgs base_step(rtm_ctx *c)
     a.rz0 = c->p.rz0; a.rx0 = c->p.rx0; a.rdz = c->p.rdz; a.rdx = c->p.rdx; a.nrec = 0;
     a.rel1 = c->rel1; a.rel2 = c->rel2; a.sacc = c->sacc; a.racc = c->racc;
     a.nxs = c->gnx; a.rx0s = c->grx0; a.vshot = c->windowed ? 1 : 0;
+    a.gbin = c->windowed ? c->mbins : c->mbin;
+    a.gbin_ss = c->windowed ? c->ss : 0;
     return a;
 }
 

@@ -115,6 +115,11 @@ struct StepArgs {
     const int *nxs, *rx0s;
     int vshot;
     int shot0;                 // first shot of this launch (blockIdx.z + shot0)
+    // the per-cell bins in global memory (the array the bin tiles are staged
+    // from; shot stride gbin_ss, 0 for the shared model): the first rows'
+    // coefficients are gathered from it before the tile's copies land
+    const int *gbin;
+    long long gbin_ss;
 };
 
 __device__ __forceinline__ int mirror_i(int i, int n)
@@ -271,9 +276,28 @@ __device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t
 // Coefficients are gathered PF rows ahead of their use (adaptive mode): a
 // gather depends on the staged velocity and usually misses L1, so issuing it
 // early hides its latency behind the rows in between.
-template <int MMAX, bool ADAPT, int MODE, int PF>
+// Coefficients of the warp's first PRE rows, gathered by each lane from the
+// global bins before the tile's copies have landed (their latency then
+// overlaps the copies instead of stalling the first rows).
+template <int MMAX, bool ADAPT, int PRE>
+__device__ __forceinline__ void pre_gather(const StepArgs &a, const float *cc, int x0, int z0, int shot,
+                                           int NX, float (&cf)[PRE > 0 ? PRE : 1][MMAX + 1])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int zw = z0 + (warp / WX) * RW, gx = x0 + (warp % WX) * 32 + lane;
+    const int *gb = a.gbin ? a.gbin + shot * a.gbin_ss : nullptr;
+#pragma unroll
+    for (int r = 0; r < PRE; ++r) {
+        int b = 0;
+        if (ADAPT && gb && zw + r < a.NZ && gx < NX) b = __ldg(gb + (long)(zw + r) * a.P + gx);
+        load_coefs<MMAX, ADAPT>(a, b, cc, cf[r]);
+    }
+}
+
+template <int MMAX, bool ADAPT, int MODE, int PF, int PRE>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX, MODE> &st,
-                                             const float *cc, int x0, int z0, int shot, int NX)
+                                             const float *cc, int x0, int z0, int shot, int NX,
+                                             const float (&cpre)[PRE > 0 ? PRE : 1][MMAX + 1])
 {
     using S = Shape<MMAX>;
     constexpr int QN = 2 * MMAX + 1;
@@ -303,7 +327,11 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     // issuing it early hides its latency behind the rows in between.
     float cfr[RW][MMAX + 1];
 #pragma unroll
-    for (int i = 0; i < PF; ++i) load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + i * TX] : 0, cc, cfr[i]);
+    for (int i = 0; i < PRE; ++i)
+#pragma unroll
+        for (int l = 0; l <= MMAX; ++l) cfr[i][l] = cpre[i][l];
+#pragma unroll
+    for (int i = PRE; i < PF; ++i) load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + i * TX] : 0, cc, cfr[i]);
 
     if (MODE == MODE_FWD) {
         // two rows per iteration: two independent accumulation chains
@@ -314,7 +342,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
         for (int i = 0; i < RW; i += 2) {
 #pragma unroll
             for (int h = 0; h < 2; ++h)
-                if (i + h + PF < RW)
+                if (i + h + PF < RW && i + h + PF >= PRE)
                     load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + h + PF) * TX] : 0, cc, cfr[i + h + PF]);
             q[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
             q[QN] = tA[(rbase + i + QN) * S::BW + cx];
@@ -360,7 +388,8 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     }
 #pragma unroll
     for (int i = 0; i < RW; ++i) {
-        if (i + PF < RW) load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + PF) * TX] : 0, cc, cfr[i + PF]);
+        if (i + PF < RW && i + PF >= PRE)
+            load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + PF) * TX] : 0, cc, cfr[i + PF]);
         qr[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
         if (rows_s) qs[QN - 1] = tS[(rbase + i + QN - 1) * S::BW + cx];
         const int z = zw + i;
@@ -437,6 +466,12 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #ifndef RTM_BWD_PF
 #define RTM_BWD_PF 2
 #endif
+#ifndef RTM_BWD_PRE
+#define RTM_BWD_PRE 2   // rows whose coefficients are gathered before the tile lands
+#endif
+#ifndef RTM_FWD_PRE
+#define RTM_FWD_PRE 2
+#endif
 #ifndef RTM_PIPE_FWD_PF
 #define RTM_PIPE_FWD_PF 2
 #endif
@@ -469,10 +504,14 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     if (threadIdx.x == 0)
         issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
                                       with_s);
-    // fixed coefficients: once per thread, while the copies are in flight
+    // fixed coefficients: once per thread, while the copies are in flight;
+    // the first rows' adaptive coefficients likewise
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
+    constexpr int PRE = !ADAPT ? 0 : (MODE == MODE_BWD ? RTM_BWD_PRE : RTM_FWD_PRE);
+    float cpre[PRE > 0 ? PRE : 1][MMAX + 1];
+    pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre);
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
     if (ok) {
         patch_halo<MMAX>(st.tA, x0, z0, NX, a.NZ);
@@ -482,7 +521,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
         return;
     }
-    compute_tile<MMAX, ADAPT, MODE, PF>(a, st, cc, x0, z0, shot, NX);
+    compute_tile<MMAX, ADAPT, MODE, PF, PRE>(a, st, cc, x0, z0, shot, NX, cpre);
 }
 
 // Forward step with two columns per lane (kernel form RTM_KERNEL_X2): the
@@ -698,7 +737,8 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
             return;
         }
         phase ^= 1u << s;
-        compute_tile<MMAX, ADAPT, MODE, PF>(a, cur, cc, x0, z0, shot, NX);
+        const float nopre[1][MMAX + 1] = {};
+        compute_tile<MMAX, ADAPT, MODE, PF, 0>(a, cur, cc, x0, z0, shot, NX, nopre);
         __syncthreads();  // every thread is done with this stage before it is reloaded
         shot = nshot; x0 = nx0; z0 = nz0;
     }
