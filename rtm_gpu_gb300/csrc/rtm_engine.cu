@@ -70,6 +70,7 @@ struct rtm_ctx {
     bool own_stream = false;  // created by the context (graphs cannot capture the legacy stream)
     cudaStream_t st2 = nullptr;           // second half-batch stream (RTM_KERNEL_SPLIT)
     cudaEvent_t evf[2] = {nullptr, nullptr};  // fork / join of the two streams
+    cudaEvent_t evc[2] = {nullptr, nullptr};  // data upload on st2: may start / done
     std::vector<float> wav; // host wavelet table
     float vmax = 0.f;
     int nbins = 1;
@@ -143,10 +144,10 @@ void free_all(rtm_ctx *c)
 {
     if (c->st2) cudaStreamDestroy(c->st2);
     c->st2 = nullptr;
-    for (cudaEvent_t &e : c->evf)
-        if (e) {
-            cudaEventDestroy(e);
-            e = nullptr;
+    for (cudaEvent_t *ev : {&c->evf[0], &c->evf[1], &c->evc[0], &c->evc[1]})
+        if (*ev) {
+            cudaEventDestroy(*ev);
+            *ev = nullptr;
         }
     for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
@@ -485,8 +486,12 @@ int enqueue_backward(rtm_ctx *c, int nb)
 int run_phase(rtm_ctx *c, int phase, int nb, int flags)
 {
     const bool use_graph = !(flags & RTM_NO_GRAPH) && !c->timing;
+    // phase 0: forward run with receiver recording; 1: forward + backward;
+    // 2: forward run of a migration; 3: its backward run
     auto body = [&]() -> int {
         if (phase == 0) return enqueue_forward(c, nb, true);
+        if (phase == 2) return enqueue_forward(c, nb, false);
+        if (phase == 3) return enqueue_backward(c, nb);
         if (int rc = enqueue_forward(c, nb, false)) return rc;
         return enqueue_backward(c, nb);
     };
@@ -618,10 +623,10 @@ __global__ void k_transpose(const float *in, float *out, int rows, int cols, lon
         if (r + j < cols && c < rows) O[(long)(r + j) * rows + c] = t[threadIdx.x][threadIdx.y + j];
 }
 
-void transpose(rtm_ctx *c, const float *in, float *out, int rows, int cols, int nb)
+void transpose(rtm_ctx *c, const float *in, float *out, int rows, int cols, int nb, cudaStream_t st)
 {
     dim3 g(cdiv(cols, 32), cdiv(rows, 32), nb);
-    k_transpose<<<g, dim3(32, 8), 0, c->st>>>(in, out, rows, cols, (long long)rows * cols);
+    k_transpose<<<g, dim3(32, 8), 0, st>>>(in, out, rows, cols, (long long)rows * cols);
     c->launches++;
 }
 
@@ -734,7 +739,9 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     }
     if (cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->evf[0], cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->evf[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->evc[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->evc[1], cudaEventDisableTiming) != cudaSuccess) {
         rtm_set_last_error("cudaStreamCreate failed");
         free_all(c);
         delete c;
@@ -1072,7 +1079,7 @@ int rtm_model_batch(rtm_ctx *c, int nshot, const int *src_cells, float *rec, int
         if (int rc = set_batch(c, nb, src_cells + s0, nullptr, nullptr)) return rc;
         if (int rc = run_phase(c, 0, nb, flags)) return rc;
         if (c->nrec > 0) {
-            transpose(c, c->rec, c->stage, c->NT, c->nrec, nb);
+            transpose(c, c->rec, c->stage, c->NT, c->nrec, nb, c->st);
             RTM_CUDA_TRY(cudaMemcpyAsync(rec + (long long)s0 * per, c->stage, sizeof(float) * per * nb,
                                          dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
         }
@@ -1094,12 +1101,18 @@ static int migrate_group(rtm_ctx *c, int s0, int nb, const int *src_cells, const
     const long long per = (long long)c->NT * c->nrec;
     if (int rc = set_batch(c, nb, src_cells + s0, xa ? xa + s0 : nullptr, nx ? nx + s0 : nullptr))
         return rc;
-    if (c->nrec > 0) {
-        RTM_CUDA_TRY(cudaMemcpyAsync(c->stage, seis + (long long)s0 * per, sizeof(float) * per * nb,
-                                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
-        transpose(c, c->stage, c->data, c->nrec, c->NT, nb);
-    }
-    return run_phase(c, 1, nb, flags);
+    if (c->nrec == 0) return run_phase(c, 1, nb, flags);
+    // The observed data are only read by the backward run: their upload and
+    // transpose go to the second stream and overlap the forward run.
+    RTM_CUDA_TRY(cudaEventRecord(c->evc[0], c->st));  // earlier users of data / stage are done
+    RTM_CUDA_TRY(cudaStreamWaitEvent(c->st2, c->evc[0], 0));
+    RTM_CUDA_TRY(cudaMemcpyAsync(c->stage, seis + (long long)s0 * per, sizeof(float) * per * nb,
+                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st2));
+    transpose(c, c->stage, c->data, c->nrec, c->NT, nb, c->st2);
+    RTM_CUDA_TRY(cudaEventRecord(c->evc[1], c->st2));
+    if (int rc = run_phase(c, 2, nb, flags)) return rc;
+    RTM_CUDA_TRY(cudaStreamWaitEvent(c->st, c->evc[1], 0));
+    return run_phase(c, 3, nb, flags);
 }
 
 int rtm_migrate_batch(rtm_ctx *c, int nshot, const int *src_cells, const float *seis, float *rel1,

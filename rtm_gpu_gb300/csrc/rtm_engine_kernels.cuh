@@ -467,7 +467,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #define RTM_BWD_PF 2
 #endif
 #ifndef RTM_BWD_PRE
-#define RTM_BWD_PRE 2   // rows whose coefficients are gathered before the tile lands
+#define RTM_BWD_PRE 6   // rows whose coefficients are gathered before the tile lands
 #endif
 #ifndef RTM_FWD_PRE
 #define RTM_FWD_PRE 2
