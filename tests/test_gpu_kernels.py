@@ -132,3 +132,24 @@ def test_split_modelling_and_fp16_rings(product_lib, cuda_ok):
     assert np.array_equal(out[TILED][0], out[SPLIT][0])
     assert np.array_equal(out[TILED][1][0], out[SPLIT][1][0])
     assert np.array_equal(out[TILED][1][1], out[SPLIT][1][1])
+
+
+def test_odd_pad_width_all_forms(product_lib, cuda_ok):
+    """An odd pad width and grid width (column pairs of the two-column
+    forward kernel straddle the pad edge): every form against the oracle."""
+    p = small_problem(nx=97, nz=41, N2=7, M=4, NT=110)
+    srcs = [p.src_flat(p.N2 + 1, p.N2 + x) for x in (0, 48, 96)]
+    seis = _seis(p, len(srcs), 13)
+    res = {}
+    with Engine(p, batch=3) as e:
+        for fwd, bwd in ((TILED, TILED), (X2, TILED), (PERSISTENT, PERSISTENT), (SPLIT, SPLIT)):
+            e.set_kernel(fwd, bwd)
+            res[(fwd, bwd)] = e.migrate(srcs, seis)
+    ref = res[(TILED, TILED)]
+    for k, (g1, g2) in res.items():
+        assert np.array_equal(g1, ref[0]) and np.array_equal(g2, ref[1]), k
+    for i, s in enumerate(srcs):
+        q = p.with_source(s // p.NX, s % p.NX)
+        o1, o2 = orc.migrate(q, seis[i])
+        assert rel_l2(interior(p, ref[0][i]), interior(p, o1)) < 1e-4
+        assert rel_l2(interior(p, ref[1][i]), interior(p, o2)) < 1e-4
