@@ -321,6 +321,10 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     const bool col_in = gx >= N2 && gx < NX - N2;
     const bool col_ok = gx < NX;
     const long long g0 = so + (long)zw * a.P + gx;  // global index of row zw
+    // every cell of the warp's rows and columns is interior and off the
+    // first interior ring: no pad stores, no per-cell predicates
+    const int xw = x0 + (warp % WX) * 32;
+    const bool inner = zw > N2 && zw + RW < NZ - N2 - 1 && xw > N2 && xw + 32 < NX - N2 - 1;
 
     // Coefficients are gathered PF rows ahead of their use (adaptive mode):
     // a gather depends on the staged velocity and usually misses L1, so
@@ -356,9 +360,11 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
                 const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cf, a.k0, a.hzx2_1);
                 float val = fmaf(fV[t], w1, 2.0f * q[MMAX + h] - fA0[t]);
                 if (i + h == src_row) val += a.wavelet;
-                if (col_ok) {
+                const long long g = g0 + (long)(i + h) * a.P;
+                if (inner) {
+                    a.a2[g] = val;
+                } else if (col_ok) {
                     const bool interior = col_in && z >= N2 && z < NZ - N2;
-                    const long long g = g0 + (long)(i + h) * a.P;
                     if (interior) a.a2[g] = val;
                     if (!interior || gx == N2 || gx == NX - 1 - N2 || z == N2 || z == NZ - 1 - N2)
                         a.pre[g] = val;
@@ -425,9 +431,11 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
                     if (d != 0.0f) rv = d;
                 }
             }
-            const bool interior = col_in && z >= N2 && z < NZ - N2;
+            const bool interior = inner || (col_in && z >= N2 && z < NZ - N2);
             const long long g = g0 + (long)i * a.P;
-            if (col_ok) {
+            if (inner) {
+                a.a2[g] = rv;
+            } else if (col_ok) {
                 if (interior) a.a2[g] = rv;
                 if (!interior || gx == N2 || gx == NX - 1 - N2 || z == N2 || z == NZ - 1 - N2)
                     a.pre[g] = rv;
