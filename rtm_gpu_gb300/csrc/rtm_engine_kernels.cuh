@@ -553,8 +553,12 @@ __device__ __forceinline__ float lap_regs(const float *q, int C, const float *xv
     return w1;
 }
 
+#ifndef RTM_X2_MINB
+#define RTM_X2_MINB 4
+#endif
+
 template <int MMAX, bool ADAPT>
-__global__ void __launch_bounds__(X2_THREADS, 4)
+__global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
     k_step_x2(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
               const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
               const __grid_constant__ ModelMaps mod, const __grid_constant__ ImgMaps img, const StepArgs a)
@@ -579,6 +583,28 @@ __global__ void __launch_bounds__(X2_THREADS, 4)
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wx = warp & 1, wz = warp >> 1;
+    const int c0 = wx * 64 + 2 * lane;        // first of the lane's two columns in the tile
+    const int gx = x0 + c0;
+    const int zw = z0 + wz * RW;
+    // coefficients of the first row pair, gathered from the global bins
+    // while the tile's copies are in flight
+    float cpa[2][MMAX + 1], cpb[2][MMAX + 1];
+    {
+        const int *gb = (ADAPT && a.gbin) ? a.gbin + shot * a.gbin_ss : nullptr;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            int ba = 0, bb = 0;
+            if (gb && zw + r < a.NZ) {
+                const int *rowb = gb + (long)(zw + r) * a.P + gx;
+                if (gx < NX) ba = __ldg(rowb);
+                if (gx + 1 < NX) bb = __ldg(rowb + 1);
+            }
+            load_coefs<MMAX, ADAPT>(a, ba, cc, cpa[r]);
+            load_coefs<MMAX, ADAPT>(a, bb, cc, cpb[r]);
+        }
+    }
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
     if (ok) patch_halo<MMAX, X2_THREADS>(st.tA, x0, z0, NX, a.NZ);
     if (!__syncthreads_and(ok)) {
@@ -587,12 +613,7 @@ __global__ void __launch_bounds__(X2_THREADS, 4)
     }
     const float *tA = st.tA, *fA0 = st.fA0, *fV = st.fV;
     const int *fB = st.fB;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int wx = warp & 1, wz = warp >> 1;
-    const int c0 = wx * 64 + 2 * lane;        // first of the lane's two columns in the tile
-    const int gx = x0 + c0;
     const int cx = S::XH + c0;                // its column in the halo box (even)
-    const int zw = z0 + wz * RW;
     const int rbase = wz * RW;
     const int fr = wz * RW * TX + c0;
     const int src = a.src[shot];
@@ -601,6 +622,10 @@ __global__ void __launch_bounds__(X2_THREADS, 4)
     const int src_row1 = (sx == gx + 1) ? src / NX - zw : -1;
     const int N2 = a.N2, NZ = a.NZ;
     const long long g0 = (long long)shot * a.ss + (long)zw * a.P + gx;
+    // every cell of the warp's rows and columns is interior and off the
+    // first interior ring: paired 8-byte stores without per-cell predicates
+    const int xw = x0 + wx * 64;
+    const bool inner = zw > N2 && zw + RW < NZ - N2 - 1 && xw > N2 && xw + 64 < NX - N2 - 1;
     float qa[QN + 1], qb[QN + 1];  // z-queues of the two columns
 #pragma unroll
     for (int j = 0; j < QN - 1; ++j) {
@@ -630,9 +655,17 @@ __global__ void __launch_bounds__(X2_THREADS, 4)
                 xv[j + 1] = v.y;
             }
             float cfa[MMAX + 1], cfb[MMAX + 1];
-            const int2 bins = ADAPT ? *reinterpret_cast<const int2 *>(fB + t) : make_int2(0, 0);
-            load_coefs<MMAX, ADAPT>(a, bins.x, cc, cfa);
-            load_coefs<MMAX, ADAPT>(a, bins.y, cc, cfb);
+            if (i == 0) {
+#pragma unroll
+                for (int l = 0; l <= MMAX; ++l) {
+                    cfa[l] = cpa[h][l];
+                    cfb[l] = cpb[h][l];
+                }
+            } else {
+                const int2 bins = ADAPT ? *reinterpret_cast<const int2 *>(fB + t) : make_int2(0, 0);
+                load_coefs<MMAX, ADAPT>(a, bins.x, cc, cfa);
+                load_coefs<MMAX, ADAPT>(a, bins.y, cc, cfb);
+            }
             const float2 vv = *reinterpret_cast<const float2 *>(fV + t);
             const float2 u0 = *reinterpret_cast<const float2 *>(fA0 + t);
             const float wa = lap_regs<MMAX, ADAPT>(qa, MMAX + h, xv, 0, cfa, a.k0, a.hzx2_1);
@@ -641,8 +674,12 @@ __global__ void __launch_bounds__(X2_THREADS, 4)
             float vb = fmaf(vv.y, wb, 2.0f * qb[MMAX + h] - u0.y);
             if (i + h == src_row0) va += a.wavelet;
             if (i + h == src_row1) vb += a.wavelet;
-            const bool zin = z >= N2 && z < NZ - N2, zring = z == N2 || z == NZ - 1 - N2;
             const long long g = g0 + (long)(i + h) * a.P;
+            if (inner) {
+                *reinterpret_cast<float2 *>(a.a2 + g) = make_float2(va, vb);
+                continue;
+            }
+            const bool zin = z >= N2 && z < NZ - N2, zring = z == N2 || z == NZ - 1 - N2;
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 const int x = gx + c;
