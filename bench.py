@@ -33,6 +33,8 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# stencil kernel forms by their RTM_KERNEL_* value
+FORMS = ["tiled", "persistent", "tiled-split", "tiled-2col", "2col-split"]
 sys.path.insert(0, ROOT)
 
 METRIC = "Gcell-updates/s"
@@ -60,7 +62,7 @@ def parse():
     ap.add_argument("--cpu-sample-nt", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split", "x2"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split", "x2", "x2-split"],
                     help="stencil kernel form (auto: the autotuner picks it and shots per launch)")
     ap.add_argument("--workload", default="multishot", choices=["multishot", "rvsp", "c5"],
                     help="rvsp: batched uneven aperture windows, well receivers, autotuned; "
@@ -291,8 +293,9 @@ def run_rvsp(a, cfg):
         tuned = eng.autotune(wsrc, xa, wn, nsteps=20)
     else:
         v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
-             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2}[a.kernel]
-        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v == capi.RTM_KERNEL_X2 else v)
+             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2,
+             "x2-split": capi.RTM_KERNEL_X2_SPLIT}[a.kernel]
+        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v in (capi.RTM_KERNEL_X2, capi.RTM_KERNEL_X2_SPLIT) else v)
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
@@ -337,8 +340,8 @@ def run_rvsp(a, cfg):
                                    % (cfg.nz, cfg.nx, nshot, rec[4], 50 + rec[4] - 1, cfg.NT,
                                       cfg.M, cfg.coef, cfg.ring.upper()),
                        "shots": nshot, "mean_window": float(np.mean(wn)), "batch": batch,
-                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["fwd"]],
-                                     "bwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["bwd"]],
+                       "autotuned": {"fwd_kernel": FORMS[kern["fwd"]],
+                                     "bwd_kernel": FORMS[kern["bwd"]],
                                      "shots_per_launch": kern["shots_per_launch"],
                                      "tuning_gcells_per_s": tuned},
                        "l2": "inputs larger than L2 (%.1f GB of wavefields and rings)"
@@ -456,8 +459,8 @@ def run_c5(a, cfg):
                                    "M=%d MLP table (optimiser fallback above 1e-4), BF16 rings"
                                    % (nshot, nt, M),
                        "shots": nshot, "nt": nt, "mean_window": float(np.mean(wn)),
-                       "autotuned": {"fwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["fwd"]],
-                                     "bwd_kernel": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["bwd"]],
+                       "autotuned": {"fwd_kernel": FORMS[kern["fwd"]],
+                                     "bwd_kernel": FORMS[kern["bwd"]],
                                      "shots_per_launch": kern["shots_per_launch"],
                                      "tuning_gcells_per_s": tuned},
                        "l2": "inputs larger than L2 (%.1f GB)" % (eng.device_bytes / 1e9)},
@@ -529,8 +532,9 @@ def main():
         tuned = eng.autotune(src, nsteps=20)
     else:
         v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
-             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2}[a.kernel]
-        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v == capi.RTM_KERNEL_X2 else v)
+             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2,
+             "x2-split": capi.RTM_KERNEL_X2_SPLIT}[a.kernel]
+        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v in (capi.RTM_KERNEL_X2, capi.RTM_KERNEL_X2_SPLIT) else v)
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
@@ -650,8 +654,8 @@ def main():
                 "steps": a.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(cfg.workload(), batch=batch,
-                               kernels={"fwd": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["fwd"]],
-                                        "bwd": ["tiled", "persistent", "tiled-split", "tiled-2col"][kern["bwd"]],
+                               kernels={"fwd": FORMS[kern["fwd"]],
+                                        "bwd": FORMS[kern["bwd"]],
                                         "shots_per_launch": kern["shots_per_launch"],
                                         "chosen_by": "autotuner" if tuned is not None else "flag",
                                         "tuning_gcells_per_s": tuned},

@@ -296,17 +296,25 @@ int rtm_ctx_launches(rtm_ctx *ctx, long *count, int reset);
  * of resident CTAs walks the batch's tiles with a two-stage TMA pipeline;
  * RTM_KERNEL_SPLIT: the tiled kernel with the two halves of a batch on two
  * streams, so one half's pad launches overlap the other's stencil launches;
- * RTM_KERNEL_X2 (forward only): the tiled kernel with two columns per lane.
+ * RTM_KERNEL_X2 (forward only): the tiled kernel with two columns per lane;
+ * RTM_KERNEL_X2_SPLIT (forward only): RTM_KERNEL_X2 on the two stream halves.
  * Set separately for the forward and the backward stencil; shots_per_launch
  * in 1..max_batch (0: max_batch). */
-enum { RTM_KERNEL_TILED = 0, RTM_KERNEL_PERSISTENT = 1, RTM_KERNEL_SPLIT = 2, RTM_KERNEL_X2 = 3 };
+enum {
+    RTM_KERNEL_TILED = 0,
+    RTM_KERNEL_PERSISTENT = 1,
+    RTM_KERNEL_SPLIT = 2,
+    RTM_KERNEL_X2 = 3,
+    RTM_KERNEL_X2_SPLIT = 4
+};
 int rtm_ctx_set_kernel(rtm_ctx *ctx, int fwd_variant, int bwd_variant, int shots_per_launch);
 int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
                        int *shots_per_launch);
 /* Autotuner: times nsteps forward and nsteps backward time steps of the
  * first shots of a survey (optional windows as rtm_migrate_stack_windows)
- * for each kernel form and for shots per launch max_batch, /2, /4, ...,
- * keeps the fastest setting in the context and returns its rate in
+ * for each kernel form (twice, interleaved, keeping each form's faster run)
+ * and for shots per launch max_batch, /2, /4, ..., keeps the fastest
+ * setting in the context and returns its rate in
  * grid-cell updates per second (/1e9).  Wavefield contents are scratch
  * afterwards. */
 int rtm_ctx_autotune(rtm_ctx *ctx, int nshot, const int *src_cells, const int *win_x0,

@@ -206,7 +206,7 @@ int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb,
     }
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
-    if (MODE == eng::MODE_FWD && c->kv[MODE] == RTM_KERNEL_X2) {
+    if (MODE == eng::MODE_FWD && (c->kv[MODE] == RTM_KERNEL_X2 || c->kv[MODE] == RTM_KERNEL_X2_SPLIT)) {
         eng::k_step_x2<MMAX, AD><<<grid, eng::X2_THREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
                                                                      c->imaps, a);
         return RTM_OK;
@@ -340,7 +340,8 @@ struct Half {
 
 int halves(rtm_ctx *c, int mode, int nb, Half h[2])
 {
-    if (c->kv[mode] == RTM_KERNEL_SPLIT && nb >= 2 && !c->timing && c->st2) {
+    const bool split = c->kv[mode] == RTM_KERNEL_SPLIT || c->kv[mode] == RTM_KERNEL_X2_SPLIT;
+    if (split && nb >= 2 && !c->timing && c->st2) {
         h[0] = Half{0, nb / 2, c->st};
         h[1] = Half{nb / 2, nb - nb / 2, c->st2};
         cudaEventRecord(c->evf[0], c->st);
@@ -971,7 +972,8 @@ int rtm_ctx_timing(const rtm_ctx *c, double ms[3], long n[3])
 int rtm_ctx_set_kernel(rtm_ctx *c, int fwd_variant, int bwd_variant, int shots_per_launch)
 {
     auto ok = [](int v) { return v == RTM_KERNEL_TILED || v == RTM_KERNEL_PERSISTENT || v == RTM_KERNEL_SPLIT; };
-    if (!c || !(ok(fwd_variant) || fwd_variant == RTM_KERNEL_X2) || !ok(bwd_variant) || shots_per_launch < 0 ||
+    const bool fwd_only = fwd_variant == RTM_KERNEL_X2 || fwd_variant == RTM_KERNEL_X2_SPLIT;
+    if (!c || !(ok(fwd_variant) || fwd_only) || !ok(bwd_variant) || shots_per_launch < 0 ||
         shots_per_launch > c->B)
         return RTM_ERR_ARG;
     if (fwd_variant != c->kv[0] || bwd_variant != c->kv[1]) {
@@ -1014,32 +1016,36 @@ int rtm_ctx_autotune(rtm_ctx *c, int nshot, const int *src_cells, const int *win
         for (int i = 0; i < nb; ++i)
             cells += (double)c->NZ * c->hnx[i] + (double)c->nz * (c->hnx[i] - 2 * c->N2);
         // tiled, persistent, tiled in two stream halves, two columns per
-        // lane (forward only: the backward form is timed as tiled there)
-        constexpr int NV = 4;
+        // lane, two columns per lane in two stream halves (the last two
+        // forward only: the backward form is timed as tiled / split there);
+        // every form timed twice, interleaved, keeping its faster run
+        constexpr int NV = 5, REPS = 2;
         double fwd_ms[NV], bwd_ms[NV];
-        for (int v = 0; v < NV && rc == RTM_OK; ++v) {
-            c->kv[0] = v;
-            c->kv[1] = v == RTM_KERNEL_X2 ? RTM_KERNEL_TILED : v;
-            c->kstop = 2 + 1;  // warm-up: one step of each phase
-            if ((rc = enqueue_forward(c, nb, false)) || (rc = enqueue_backward(c, nb))) break;
-            c->kstop = 2 + nsteps;
-            cudaEventRecord(e[0], c->st);
-            if ((rc = enqueue_forward(c, nb, false))) break;
-            cudaEventRecord(e[1], c->st);
-            if ((rc = enqueue_backward(c, nb))) break;
-            cudaEventRecord(e[2], c->st);
-            if (cudaEventSynchronize(e[2]) != cudaSuccess) { rc = RTM_ERR_CUDA; break; }
-            float a = 0, b = 0;
-            cudaEventElapsedTime(&a, e[0], e[1]);
-            cudaEventElapsedTime(&b, e[1], e[2]);
-            fwd_ms[v] = a;
-            bwd_ms[v] = b;
-        }
+        for (int v = 0; v < NV; ++v) fwd_ms[v] = bwd_ms[v] = 1e30;
+        for (int rep = 0; rep < REPS && rc == RTM_OK; ++rep)
+            for (int v = 0; v < NV && rc == RTM_OK; ++v) {
+                c->kv[0] = v;
+                c->kv[1] = v == RTM_KERNEL_X2 ? RTM_KERNEL_TILED : v == RTM_KERNEL_X2_SPLIT ? RTM_KERNEL_SPLIT : v;
+                c->kstop = 2 + 1;  // warm-up: one step of each phase
+                if ((rc = enqueue_forward(c, nb, false)) || (rc = enqueue_backward(c, nb))) break;
+                c->kstop = 2 + nsteps;
+                cudaEventRecord(e[0], c->st);
+                if ((rc = enqueue_forward(c, nb, false))) break;
+                cudaEventRecord(e[1], c->st);
+                if ((rc = enqueue_backward(c, nb))) break;
+                cudaEventRecord(e[2], c->st);
+                if (cudaEventSynchronize(e[2]) != cudaSuccess) { rc = RTM_ERR_CUDA; break; }
+                float a = 0, b = 0;
+                cudaEventElapsedTime(&a, e[0], e[1]);
+                cudaEventElapsedTime(&b, e[1], e[2]);
+                fwd_ms[v] = std::min(fwd_ms[v], (double)a);
+                bwd_ms[v] = std::min(bwd_ms[v], (double)b);
+            }
         if (rc) break;
         int vf = 0, vb = 0;
         for (int v = 1; v < NV; ++v) {
             if (fwd_ms[v] < fwd_ms[vf]) vf = v;
-            if (v != RTM_KERNEL_X2 && bwd_ms[v] < bwd_ms[vb]) vb = v;
+            if (v != RTM_KERNEL_X2 && v != RTM_KERNEL_X2_SPLIT && bwd_ms[v] < bwd_ms[vb]) vb = v;
         }
         const double rate = cells * nsteps / ((fwd_ms[vf] + bwd_ms[vb]) * 1e-3) / 1e9;
         if (rate > best) {

@@ -61,8 +61,9 @@ class Engine:
         return int(n.value)
 
     def set_kernel(self, fwd: int, bwd: int | None = None, shots_per_launch: int = 0):
-        """Stencil kernel form per phase (capi.RTM_KERNEL_TILED / _PERSISTENT)
-        and shots per launch (0: the context's batch)."""
+        """Stencil kernel form per phase (capi.RTM_KERNEL_TILED / _PERSISTENT /
+        _SPLIT; the forward also _X2 / _X2_SPLIT) and shots per launch (0: the
+        context's batch)."""
         bwd = fwd if bwd is None else bwd
         capi.check(capi.lib().rtm_ctx_set_kernel(self._h, fwd, bwd, shots_per_launch), "set_kernel")
 

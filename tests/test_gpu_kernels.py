@@ -12,8 +12,8 @@ from test_gpu_windows import window_problem
 from util import interior, rel_l2, small_problem
 
 pytestmark = pytest.mark.gpu
-TILED, PERSISTENT, SPLIT, X2 = (capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_PERSISTENT, capi.RTM_KERNEL_SPLIT,
-                                capi.RTM_KERNEL_X2)
+TILED, PERSISTENT, SPLIT, X2, X2S = (capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_PERSISTENT, capi.RTM_KERNEL_SPLIT,
+                                     capi.RTM_KERNEL_X2, capi.RTM_KERNEL_X2_SPLIT)
 
 
 def _seis(p, n, seed):
@@ -29,7 +29,7 @@ def test_forms_bit_identical(product_lib, cuda_ok, adaptive):
     out = {}
     with Engine(p, batch=5) as e:
         for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (TILED, PERSISTENT), (SPLIT, SPLIT),
-                         (PERSISTENT, SPLIT), (X2, TILED)):
+                         (PERSISTENT, SPLIT), (X2, TILED), (X2S, SPLIT), (X2S, TILED)):
             e.set_kernel(fwd, bwd)
             assert e.kernel() == {"fwd": fwd, "bwd": bwd, "shots_per_launch": 5}
             out[(fwd, bwd)] = e.migrate(srcs, seis)
@@ -49,7 +49,7 @@ def test_forms_bit_identical_uneven_windows(product_lib, cuda_ok):
     seis = _seis(p, len(wins), 4)
     res = []
     with Engine(p, batch=5) as e:
-        for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (SPLIT, SPLIT), (X2, TILED)):
+        for fwd, bwd in ((TILED, TILED), (PERSISTENT, PERSISTENT), (SPLIT, SPLIT), (X2, TILED), (X2S, TILED)):
             e.set_kernel(fwd, bwd)
             res.append(e.migrate_stack_windows(srcs, [w[0] for w in wins], [w[1] for w in wins],
                                                seis, 1e-4, len(wins), True))
