@@ -45,6 +45,18 @@ def cell_updates_per_shot(nz, nx, N2, NT):
     return NT * (2 * NZ * NX + nz * nx)
 
 
+def kernel_forms(a):
+    """(forward, backward) stencil forms of --kernel / --bwd-kernel."""
+    from rtm_gpu_gb300 import capi
+    v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
+         "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2,
+         "x2-split": capi.RTM_KERNEL_X2_SPLIT}
+    f = v[a.kernel]
+    if a.bwd_kernel != "same":
+        return f, v[a.bwd_kernel]
+    return f, capi.RTM_KERNEL_TILED if f in (capi.RTM_KERNEL_X2, capi.RTM_KERNEL_X2_SPLIT) else f
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -64,6 +76,8 @@ def parse():
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
     ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split", "x2", "x2-split"],
                     help="stencil kernel form (auto: the autotuner picks it and shots per launch)")
+    ap.add_argument("--bwd-kernel", default="same", choices=["same", "tiled", "persistent", "split"],
+                    help="backward stencil form with a fixed --kernel (same: --kernel's, tiled for x2 forms)")
     ap.add_argument("--workload", default="multishot", choices=["multishot", "rvsp", "c5"],
                     help="rvsp: batched uneven aperture windows, well receivers, autotuned; "
                          "c5: learned coefficients, 1201x4001 model, BF16 rings, uneven apertures")
@@ -292,10 +306,7 @@ def run_rvsp(a, cfg):
     if a.kernel == "auto":
         tuned = eng.autotune(wsrc, xa, wn, nsteps=20)
     else:
-        v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
-             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2,
-             "x2-split": capi.RTM_KERNEL_X2_SPLIT}[a.kernel]
-        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v in (capi.RTM_KERNEL_X2, capi.RTM_KERNEL_X2_SPLIT) else v)
+        eng.set_kernel(*kernel_forms(a))
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
@@ -531,10 +542,7 @@ def main():
     if a.kernel == "auto":
         tuned = eng.autotune(src, nsteps=20)
     else:
-        v = {"tiled": capi.RTM_KERNEL_TILED, "persistent": capi.RTM_KERNEL_PERSISTENT,
-             "split": capi.RTM_KERNEL_SPLIT, "x2": capi.RTM_KERNEL_X2,
-             "x2-split": capi.RTM_KERNEL_X2_SPLIT}[a.kernel]
-        eng.set_kernel(v, capi.RTM_KERNEL_TILED if v in (capi.RTM_KERNEL_X2, capi.RTM_KERNEL_X2_SPLIT) else v)
+        eng.set_kernel(*kernel_forms(a))
     kern = eng.kernel()
     img = torch.zeros((pmig.nz, pmig.nx), dtype=torch.float32, device="cuda")
     ill = torch.zeros_like(img)
