@@ -43,3 +43,17 @@ def test_ring_bytes_halved(product_lib, cuda_ok, case):
             Engine(p, batch=1, ring_precision=capi.RTM_RING_BF16) as b:
         ring32 = p.NT * 2 * p.M * (p.nz + p.nx) * 4
         assert a.device_bytes - b.device_bytes >= 0.45 * ring32
+
+
+@pytest.mark.parametrize("prec", [capi.RTM_RING_F32, capi.RTM_RING_F16, capi.RTM_RING_BF16])
+def test_gathers_vs_fp64(product_lib, cuda_ok, case, prec):
+    """Shot gathers of the forward run against the FP64 oracle for each ring
+    storage precision (the rings enter only the backward run, so the
+    gathers carry the FP32 arithmetic's error alone)."""
+    p = case[0]
+    ref = orc.model(p, precision="f64")
+    with Engine(p, batch=1, ring_precision=prec) as e:
+        g = e.model([p.src_flat()])[0]
+    err = rel_l2(g, ref)
+    print("ring precision %d: gather rel-L2 %.3e" % (prec, err))
+    assert err <= 1e-3
