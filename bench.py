@@ -67,8 +67,9 @@ def parse():
     ap.add_argument("--nt", type=int, default=4000)
     ap.add_argument("--batch", type=int, default=0, help="shots per batch (0: all)")
     ap.add_argument("--coef", default="adaptive", choices=["adaptive", "taylor"])
-    ap.add_argument("--ring", default="f16", choices=["f32", "bf16", "f16"],
-                    help="boundary-ring storage (stencil and imaging stay FP32)")
+    ap.add_argument("--ring", default=None, choices=["f32", "bf16", "f16"],
+                    help="boundary-ring storage (stencil and imaging stay FP32); default f16 "
+                         "for the multi-shot workload, f32 for rvsp (FP32 throughout), bf16 for c5")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip timing the plain single-shot drop-in for comparison")
     ap.add_argument("--cpu-sample-nt", type=int, default=0)
@@ -93,7 +94,7 @@ class Config:
         self.NT = a.nt
         self.nshot = a.shots
         self.coef = a.coef
-        self.ring = a.ring
+        self.ring = a.ring or {"multishot": "f16", "rvsp": "f32", "c5": "bf16"}[a.workload]
         self.whitecoe = 1e-4
         # optimiser settings (the reference's parameter file: nthita=1000,
         # eps=1e-5, df=1; fmax = 2*f0)
