@@ -7,8 +7,9 @@ import numpy as np
 import pytest
 
 from oracle import oracle as orc
-from rtm_gpu_gb300 import Engine
-from util import interior, rel_l2, small_problem
+from rtm_gpu_gb300 import Engine, capi
+from rtm_gpu_gb300.problem import build_problem, prep_taylor
+from util import interior, layered_model, rel_l2, small_problem
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
@@ -50,6 +51,64 @@ def test_taylor_long_operators(product_lib, cuda_ok, M, eps_nt):
         g1, g2 = e.migrate([p.src_flat()], seis[None])
     assert rel_l2(interior(p, g1[0]), interior(p, o1)) < TOL
     assert rel_l2(interior(p, g2[0]), interior(p, o2)) < TOL
+
+
+def _long_table(vmin, dv, nvel, need, hzx):
+    """Per-bin table of the longest operators (Taylor coefficients of M=9 and
+    M=10 on alternate bins): the least-squares optimiser's own M=10 designs
+    on a test-sized grid come from ill-conditioned normal equations (|c| in
+    the thousands) and blow up in the reference's own code as well."""
+    taylor = {9: prep_taylor(9), 10: prep_taylor(10)}
+    length = np.zeros(nvel, np.int32)
+    index = np.zeros(nvel + 1, np.int32)
+    coef, n = [], 0
+    for b in range(nvel):
+        index[b] = n
+        if need[b]:
+            c = taylor[10 if b % 2 else 9]
+            length[b] = len(c) - 1
+            coef.extend(c)
+            n += len(c)
+    index[nvel] = n
+    return length, index, np.asarray(coef, np.float32)
+
+
+def long_operator_problem():
+    """Adaptive (per-bin) coefficients of operator length 9 and 10 -- the
+    longest of the C5 range, run by the kernels' 12-wide instantiation."""
+    N2, M, nz, nx, tao, h, f0 = 12, 10, 48, 150, 0.001, 10.0, 25.0
+    vin = layered_model(nz, nx, 1500.0, 3500.0, 1)
+    p = build_problem(vin, N2=N2, M=M, NT=160, h=h, tao=tao, f0=f0, adaptive=True, compen=True,
+                      rec=(N2 + 1, N2, 0, 2, (nx + 1) // 2), coef_table=_long_table)
+    assert set(np.diff(p.index)) == {0, 10, 11}
+    return p.with_source(N2 + 2, N2 + nx // 2)
+
+
+def test_adaptive_long_operators(product_lib, cuda_ok):
+    p = long_operator_problem()
+    seis = _seis(p, 5)
+    o1, o2 = orc.migrate(p, seis)
+    with Engine(p, batch=1) as e:
+        g1, g2 = e.migrate([p.src_flat()], seis[None])
+        rec = e.model([p.src_flat()])[0]
+    assert rel_l2(interior(p, g1[0]), interior(p, o1)) < TOL
+    assert rel_l2(interior(p, g2[0]), interior(p, o2)) < TOL
+    assert rel_l2(rec, orc.model(p)) < TOL
+
+
+def test_adaptive_long_operators_forms(product_lib, cuda_ok):
+    p = long_operator_problem()
+    srcs = [p.src_flat(p.N2 + 1, p.N2 + x) for x in (3, 77, 149)]
+    seis = np.stack([_seis(p, s) for s in range(len(srcs))])
+    out = []
+    with Engine(p, batch=3) as e:
+        for fwd, bwd in ((capi.RTM_KERNEL_TILED, capi.RTM_KERNEL_TILED),
+                         (capi.RTM_KERNEL_PERSISTENT, capi.RTM_KERNEL_PERSISTENT),
+                         (capi.RTM_KERNEL_X2_SPLIT, capi.RTM_KERNEL_SPLIT)):
+            e.set_kernel(fwd, bwd)
+            out.append(e.migrate(srcs, seis))
+    for g in out[1:]:
+        assert np.array_equal(g[0], out[0][0]) and np.array_equal(g[1], out[0][1])
 
 
 def test_batch_of_shots_matches_single(product_lib, cuda_ok):
