@@ -297,7 +297,8 @@ __device__ __forceinline__ void pre_gather(const StepArgs &a, const float *cc, i
 template <int MMAX, bool ADAPT, int MODE, int PF, int PRE>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX, MODE> &st,
                                              const float *cc, int x0, int z0, int shot, int NX,
-                                             const float (&cpre)[PRE > 0 ? PRE : 1][MMAX + 1])
+                                             const float (&cpre)[PRE > 0 ? PRE : 1][MMAX + 1],
+                                             int src, int rx0)
 {
     using S = Shape<MMAX>;
     constexpr int QN = 2 * MMAX + 1;
@@ -306,7 +307,6 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     const float *fR1 = st.fR1, *fR2 = st.fR2, *fSa = st.fSa, *fRa = st.fRa;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wx = warp % WX, wz = warp / WX;
-    const int src = a.src[shot];
     const long long so = (long long)shot * a.ss;
     const int zw = z0 + wz * RW;             // first row of this warp
     const int gx = x0 + wx * 32 + lane;      // this lane's column
@@ -317,7 +317,6 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     // the source is not in this column)
     const int src_row = (src % NX == x0 + wx * 32 + lane) ? src / NX - (z0 + wz * RW) : -1;
     const int N2 = a.N2, NZ = a.NZ;
-    const int rx0 = a.rx0s[shot];
     const bool col_in = gx >= N2 && gx < NX - N2;
     const bool col_ok = gx < NX;
     const long long g0 = so + (long)zw * a.P + gx;  // global index of row zw
@@ -500,18 +499,19 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     const Stage<MMAX, MODE> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
-    const int NX = a.nxs[shot];
+    // the shot's width: a load only when shots have their own windows, so
+    // that nothing delays the tile's copies otherwise
+    const int NX = a.vshot ? a.nxs[shot] : a.NX;
     if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
 
+    const bool with_s = tile_has_interior_rows(z0, a.NZ, a.N2);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
-    }
-    __syncthreads();
-    const bool with_s = tile_has_interior_rows(z0, a.NZ, a.N2);
-    if (threadIdx.x == 0)
         issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
                                       with_s);
+    }
+    __syncthreads();  // the barrier is initialised before any thread waits on it
     // fixed coefficients: once per thread, while the copies are in flight;
     // the first rows' adaptive coefficients likewise
     float cc[MMAX + 1];
@@ -520,6 +520,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     constexpr int PRE = !ADAPT ? 0 : (MODE == MODE_BWD ? RTM_BWD_PRE : RTM_FWD_PRE);
     float cpre[PRE > 0 ? PRE : 1][MMAX + 1];
     pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre);
+    const int src = __ldg(a.src + shot), rx0 = MODE == MODE_BWD ? __ldg(a.rx0s + shot) : 0;
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
     if (ok) {
         patch_halo<MMAX>(st.tA, x0, z0, NX, a.NZ);
@@ -529,7 +530,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
         return;
     }
-    compute_tile<MMAX, ADAPT, MODE, PF, PRE>(a, st, cc, x0, z0, shot, NX, cpre);
+    compute_tile<MMAX, ADAPT, MODE, PF, PRE>(a, st, cc, x0, z0, shot, NX, cpre, src, rx0);
 }
 
 // Forward step with two columns per lane (kernel form RTM_KERNEL_X2): the
@@ -570,16 +571,15 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
     const Stage<MMAX, MODE_FWD> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE_FWD>());
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
-    const int NX = a.nxs[shot];
+    const int NX = a.vshot ? a.nxs[shot] : a.NX;
     if (x0 >= NX) return;
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
         issue_tile<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot,
                                           a.vshot, false);
+    }
+    __syncthreads();  // the barrier is initialised before any thread waits on it
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
@@ -605,6 +605,7 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
             load_coefs<MMAX, ADAPT>(a, bb, cc, cpb[r]);
         }
     }
+    const int src = __ldg(a.src + shot);
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
     if (ok) patch_halo<MMAX, X2_THREADS>(st.tA, x0, z0, NX, a.NZ);
     if (!__syncthreads_and(ok)) {
@@ -616,7 +617,6 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
     const int cx = S::XH + c0;                // its column in the halo box (even)
     const int rbase = wz * RW;
     const int fr = wz * RW * TX + c0;
-    const int src = a.src[shot];
     const int sx = src % NX;
     const int src_row0 = (sx == gx) ? src / NX - zw : -1;
     const int src_row1 = (sx == gx + 1) ? src / NX - zw : -1;
@@ -783,7 +783,8 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
         }
         phase ^= 1u << s;
         const float nopre[1][MMAX + 1] = {};
-        compute_tile<MMAX, ADAPT, MODE, PF, 0>(a, cur, cc, x0, z0, shot, NX, nopre);
+        compute_tile<MMAX, ADAPT, MODE, PF, 0>(a, cur, cc, x0, z0, shot, NX, nopre, __ldg(a.src + shot),
+                                               __ldg(a.rx0s + shot));
         __syncthreads();  // every thread is done with this stage before it is reloaded
         shot = nshot; x0 = nx0; z0 = nz0;
     }
@@ -934,7 +935,6 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int shot = blockIdx.y + a.shot0;
     const long long so = (long long)shot * a.ss;
-    const int NX = a.nxs[shot];
     const long npadt = (a.nabc + PAD_CPT - 1) / PAD_CPT;  // threads of the pad cells
     if (t >= npadt) {
         long j = t - npadt;
@@ -953,7 +953,9 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         }
         return;
     }
-    const long nmine = abc_count(a.NZ, NX, a.N2);  // this shot's pad may be smaller
+    // this shot's pad may be smaller (own window); with one shared table
+    // every shot has the full pad, and no width load delays the cells
+    const long nmine = a.tab_ss ? abc_count(a.NZ, a.nxs[shot], a.N2) : a.nabc;
     PadOut r[PAD_CPT];
     bool on[PAD_CPT];
 #pragma unroll
