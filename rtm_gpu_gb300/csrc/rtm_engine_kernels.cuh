@@ -137,7 +137,7 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
     const int gx0 = x0 - S::XH, gz0 = z0 - S::ZH;
     // x reflection on the tile's in-grid rows, z reflection on its in-grid
     // columns: the written and the read cells of the two passes never overlap.
-    if (x0 == 0 || x0 + TX + S::XH > NX) {
+    if (x0 == 0 || x0 + TX + S::XH > NX) {  // the conditions of tile_at_edge
         for (int idx = threadIdx.x; idx < TZ * S::BW; idx += NT) {
             const int r = S::ZH + idx / S::BW, c = idx % S::BW;
             const int gx = gx0 + c, gz = gz0 + r;
@@ -155,6 +155,14 @@ __device__ __forceinline__ void patch_halo(float *t, int x0, int z0, int NX, int
             t[r * S::BW + c] = (sr >= 0 && sr < S::BH) ? t[sr * S::BW + c] : 0.0f;
         }
     }
+}
+
+// Whether a tile's halo box reaches past the grid (patch_halo has work).
+template <int MMAX>
+__device__ __forceinline__ bool tile_at_edge(int x0, int z0, int NX, int NZ)
+{
+    using S = Shape<MMAX>;
+    return x0 == 0 || x0 + TX + S::XH > NX || z0 == 0 || z0 + TZ + S::ZH > NZ;
 }
 
 // Layout of the adaptive table: coefficient-major (float4 group q of bin b
@@ -511,9 +519,9 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
                                       with_s);
     }
-    __syncthreads();  // the barrier is initialised before any thread waits on it
     // fixed coefficients: once per thread, while the copies are in flight;
-    // the first rows' adaptive coefficients likewise
+    // the first rows' adaptive coefficients likewise (issued by every thread
+    // while thread 0 is still issuing the copies)
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
@@ -521,13 +529,21 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     float cpre[PRE > 0 ? PRE : 1][MMAX + 1];
     pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre);
     const int src = __ldg(a.src + shot), rx0 = MODE == MODE_BWD ? __ldg(a.rx0s + shot) : 0;
+    __syncthreads();  // the barrier is initialised before any thread waits on it
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
-    if (ok) {
-        patch_halo<MMAX>(st.tA, x0, z0, NX, a.NZ);
-        if (MODE == MODE_BWD && with_s) patch_halo<MMAX>(st.tS, x0, z0, NX, a.NZ);
-    }
-    if (!__syncthreads_and(ok)) {
-        mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
+    if (tile_at_edge<MMAX>(x0, z0, NX, a.NZ)) {
+        // out-of-grid halo mirrored by all threads before any reads it
+        if (ok) {
+            patch_halo<MMAX>(st.tA, x0, z0, NX, a.NZ);
+            if (MODE == MODE_BWD && with_s) patch_halo<MMAX>(st.tS, x0, z0, NX, a.NZ);
+        }
+        if (!__syncthreads_and(ok)) {
+            mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);  // let an in-flight copy land before exit
+            return;
+        }
+    } else if (!ok) {
+        // no halo to mirror: every warp starts as soon as its own wait is over
+        mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
         return;
     }
     compute_tile<MMAX, ADAPT, MODE, PF, PRE>(a, st, cc, x0, z0, shot, NX, cpre, src, rx0);
@@ -579,7 +595,6 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
         issue_tile<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot,
                                           a.vshot, false);
     }
-    __syncthreads();  // the barrier is initialised before any thread waits on it
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
@@ -606,9 +621,15 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
         }
     }
     const int src = __ldg(a.src + shot);
+    __syncthreads();  // the barrier is initialised before any thread waits on it
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
-    if (ok) patch_halo<MMAX, X2_THREADS>(st.tA, x0, z0, NX, a.NZ);
-    if (!__syncthreads_and(ok)) {
+    if (tile_at_edge<MMAX>(x0, z0, NX, a.NZ)) {
+        if (ok) patch_halo<MMAX, X2_THREADS>(st.tA, x0, z0, NX, a.NZ);
+        if (!__syncthreads_and(ok)) {
+            mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
+            return;
+        }
+    } else if (!ok) {
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
         return;
     }
