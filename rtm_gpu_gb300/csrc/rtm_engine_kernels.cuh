@@ -525,7 +525,9 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     float cc[MMAX + 1];
 #pragma unroll
     for (int l = 0; l <= MMAX; ++l) cc[l] = ADAPT ? 0.0f : __ldg(a.ctab + l);
-    constexpr int PRE = !ADAPT ? 0 : (MODE == MODE_BWD ? RTM_BWD_PRE : RTM_FWD_PRE);
+    // (the 12-wide backward gathers two rows early: six rows of 13
+    // coefficients would not fit its registers)
+    constexpr int PRE = !ADAPT ? 0 : (MODE == MODE_BWD ? (MMAX <= 8 ? RTM_BWD_PRE : 2) : RTM_FWD_PRE);
     float cpre[PRE > 0 ? PRE : 1][MMAX + 1];
     pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre);
     const int src = __ldg(a.src + shot), rx0 = MODE == MODE_BWD ? __ldg(a.rx0s + shot) : 0;
