@@ -266,6 +266,32 @@ def rvsp_geometry(cfg, nshot=128, seed=1237, wmin=300, wmax=1201, well_x=600, z0
     return src, xa.astype(np.int32), w.astype(np.int32), (N2 + z0, N2 + well_x, 1, 0, nrec)
 
 
+def windowed_roofline(eng, step, NZ, nz, N2, wn, nbl):
+    """Roofline of the backward stencil (the dominant kernel) for shots of
+    uneven windows: the algorithmic bytes of all its launches in one
+    migration (per launch and shot: 16 B per receiver-field cell of the
+    padded window, 16 B per source-field cell and 32 B of compensated
+    imaging per interior cell) over their summed CUDA-event durations."""
+    eng.set_timing(True)
+    step()
+    tm = eng.timing()
+    eng.set_timing(False)
+    nbatch = -(-len(wn) // nbl)
+    steps = tm["bwd_n"] / max(nbatch, 1)  # backward launches of one batch
+    bwd_step = sum(16 * (NZ * (int(w) + 2 * N2) + nz * int(w)) + 32 * nz * int(w) for w in wn)
+    fwd_step = sum(16 * NZ * (int(w) + 2 * N2) for w in wn)
+    achieved = bwd_step * steps / (tm["bwd_ms"] / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None,
+            "kernel": "k_step<backward> (source reconstruction + receiver step + imaging)",
+            "bytes_per_launch": bwd_step / max(nbatch, 1), "launch_ms": tm["bwd_ms"] / max(tm["bwd_n"], 1),
+            "peak_kind": peak_kind,
+            "forward_kernel": {"launch_ms": tm["fwd_ms"] / max(tm["fwd_n"], 1),
+                               "achieved": fwd_step * steps / (tm["fwd_ms"] / 1e3) / 1e9},
+            "pad_kernel_ms": tm["pad_ms"] / max(tm["pad_n"], 1)}
+
+
 def run_rvsp(a, cfg):
     """Batched uneven shots (reverse VSP): all shots' windows advance
     together; kernel form and shots per launch from the autotuner; FP32."""
@@ -343,6 +369,7 @@ def run_rvsp(a, cfg):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1) / a.steps
+    roofline = windowed_roofline(eng, step, NZ, cfg.nz, cfg.N2, wn, kern["shots_per_launch"])
     line = {"metric": METRIC, "value": cu / (ms / 1e3) / 1e9, "unit": METRIC, "n_gpus": 1,
             "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -362,6 +389,7 @@ def run_rvsp(a, cfg):
             "e2e": {"value": cu / (ms_e2e / 1e3) / 1e9, "unit": METRIC,
                     "h2d_bytes_per_step": int(seis_h.numel() * 4),
                     "d2h_bytes_per_step": int((img_h.numel() + ill_h.numel()) * 4)},
+            "roofline": roofline,
             "clocks": clk.summary(0), "gpu_launches": launches,
             "gpu_launches_per_step": launches // a.steps}
     print(json.dumps(line))
@@ -459,9 +487,11 @@ def run_c5(a, cfg):
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / a.steps
+    launches = eng.launches()
     NZ = nz + 2 * N2
     cu = sum(nt * (2 * NZ * (int(w) + 2 * N2) + nz * int(w)) for w in wn)
     used = info["err_used"][sel]
+    roofline = windowed_roofline(eng, step, NZ, nz, N2, wn, kern["shots_per_launch"])
     line = {"metric": METRIC, "value": cu / (ms / 1e3) / 1e9, "unit": METRIC, "n_gpus": 1,
             "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -482,7 +512,8 @@ def run_c5(a, cfg):
                              "max_dispersion_error_table": float(used.max()),
                              "network_train_s": t_train, "network_train_loss": train_loss,
                              "table_s": info["seconds"], "optimiser_alone_s": t_opt},
-            "clocks": clk.summary(0), "gpu_launches": eng.launches()}
+            "roofline": roofline,
+            "clocks": clk.summary(0), "gpu_launches": launches}
     print(json.dumps(line))
     eng.close()
 
