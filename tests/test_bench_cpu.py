@@ -54,3 +54,30 @@ def test_defaults_keep_the_contract():
     a = _args()
     assert a.gpus == 1 and a.warmup >= 3 and a.steps >= 1 and a.impl == "ours"
     assert a.kernel == "auto" and a.workload == "multishot"
+
+
+class _FakeEngine:
+    """Timing counters of one migration of two batches: 10 backward and 10
+    forward launches per batch, 2 ms and 1 ms each, 0.5 ms per pad launch."""
+
+    def __init__(self):
+        self.on = False
+
+    def set_timing(self, on):
+        self.on = on
+
+    def timing(self):
+        return {"fwd_ms": 20 * 1.0, "bwd_ms": 20 * 2.0, "pad_ms": 40 * 0.5,
+                "fwd_n": 20, "bwd_n": 20, "pad_n": 40}
+
+
+def test_windowed_roofline_counts_every_shot_once_per_step(monkeypatch):
+    monkeypatch.setattr(bench, "measured_peak", lambda: (1000.0, "measured"))
+    NZ, nz, N2, wn = 40, 30, 5, [20, 10, 30]
+    r = bench.windowed_roofline(_FakeEngine(), lambda: None, NZ, nz, N2, wn, nbl=2)
+    per_step = sum(16 * (NZ * (w + 2 * N2) + nz * w) + 32 * nz * w for w in wn)
+    # 2 batches of 10 backward steps: each shot 10 steps, 40 ms in all
+    assert r["achieved"] == pytest.approx(per_step * 10 / 0.040 / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved"] / 1000.0)
+    assert r["launch_ms"] == pytest.approx(2.0) and r["pad_kernel_ms"] == pytest.approx(0.5)
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s"
