@@ -291,13 +291,15 @@ int rtm_ctx_timing(const rtm_ctx *ctx, double ms[3], long n[3]);
 int rtm_ctx_launches(rtm_ctx *ctx, long *count, int reset);
 
 /* Stencil kernel form and shots per launch (no reference counterpart: the
- * reference launches one shot at a time).  RTM_KERNEL_TILED: one CTA per
- * 128 x 16 tile of every shot; RTM_KERNEL_PERSISTENT (default): a fixed grid
- * of resident CTAs walks the batch's tiles with a two-stage TMA pipeline;
+ * reference launches one shot at a time).  RTM_KERNEL_TILED (the backward
+ * default): one CTA per 128 x 16 tile of every shot; RTM_KERNEL_PERSISTENT:
+ * a fixed grid of resident CTAs walks the batch's tiles with a two-stage TMA
+ * pipeline;
  * RTM_KERNEL_SPLIT: the tiled kernel with the two halves of a batch on two
  * streams, so one half's pad launches overlap the other's stencil launches;
  * RTM_KERNEL_X2 (forward only): the tiled kernel with two columns per lane;
- * RTM_KERNEL_X2_SPLIT (forward only): RTM_KERNEL_X2 on the two stream halves.
+ * RTM_KERNEL_X2_SPLIT (forward only; the forward default): RTM_KERNEL_X2 on
+ * the two stream halves.  All forms give bit-identical results.
  * Set separately for the forward and the backward stencil; shots_per_launch
  * in 1..max_batch (0: max_batch). */
 enum {

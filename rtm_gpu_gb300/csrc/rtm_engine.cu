@@ -103,7 +103,9 @@ struct rtm_ctx {
     int *gnx = nullptr, *gxa = nullptr, *grx0 = nullptr;
     int *gitem = nullptr;              // [B+1] first tile item of each shot (persistent kernel)
     std::vector<int> hnx, hxa;         // host copies for the current batch
-    int kv[2] = {RTM_KERNEL_PERSISTENT, RTM_KERNEL_PERSISTENT};  // stencil kernel form (fwd, bwd)
+    // stencil kernel form (fwd, bwd): the forms the autotuner picks on the
+    // batched workloads, until it or rtm_ctx_set_kernel sets others
+    int kv[2] = {RTM_KERNEL_X2_SPLIT, RTM_KERNEL_TILED};
     int nbl = 0;                           // shots per launch (<= B)
     int kstop = 0;                         // autotuning: time steps per phase (0: all)
     bool windowed = false;             // current batch uses per-shot models

@@ -78,7 +78,7 @@ def test_autotune_then_oracle(product_lib, cuda_ok):
         rate = e.autotune(srcs, nsteps=10)
         k = e.kernel()
         assert rate > 0
-        assert k["fwd"] in (TILED, PERSISTENT, SPLIT, X2) and k["bwd"] in (TILED, PERSISTENT, SPLIT)
+        assert k["fwd"] in (TILED, PERSISTENT, SPLIT, X2, X2S) and k["bwd"] in (TILED, PERSISTENT, SPLIT)
         assert k["shots_per_launch"] in (8, 4)
         g1, g2 = e.migrate(srcs, seis)
     for i in (0, 5, 7):
