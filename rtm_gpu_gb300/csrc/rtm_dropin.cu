@@ -457,7 +457,10 @@ struct DevArr {
             rtm_set_last_error("cudaMalloc failed");
             return RTM_ERR_NOMEM;
         }
-        cudaMemset(p, 0, sizeof(T) * (n ? n : 1));
+        if (cudaMemset(p, 0, sizeof(T) * (n ? n : 1)) != cudaSuccess) {
+            rtm_set_last_error("cudaMemset failed");
+            return RTM_ERR_CUDA;
+        }
         return RTM_OK;
     }
 };
