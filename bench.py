@@ -33,6 +33,9 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# time steps of the CPU baseline's one-shot sample (about 10 s of the
+# reference's kernel bodies on 16 host cores for the multi-shot grid)
+CPU_SAMPLE_NT = 2000
 # stencil kernel forms by their RTM_KERNEL_* value
 FORMS = ["tiled", "persistent", "tiled-split", "tiled-2col", "2col-split"]
 sys.path.insert(0, ROOT)
@@ -72,7 +75,9 @@ def parse():
                          "for the multi-shot workload, f32 for rvsp (FP32 throughout), bf16 for c5")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip timing the plain single-shot drop-in for comparison")
-    ap.add_argument("--cpu-sample-nt", type=int, default=0)
+    ap.add_argument("--cpu-sample-nt", type=int, default=0,
+                    help="time steps of the one-shot CPU sample (0: %d, about 10 s on 16 cores)"
+                         % CPU_SAMPLE_NT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
     ap.add_argument("--kernel", default="auto", choices=["auto", "tiled", "persistent", "split", "x2", "x2-split"],
@@ -228,7 +233,7 @@ def run_reference_arm(a, cfg):
     # the reference arm needs no GPU: a Taylor problem of the same grid for
     # the loop (coefficient count M=8 per cell as the adaptive table at M=8)
     vmig = synth.smooth_model(synth.model_c2(nz=cfg.nz, nx=cfg.nx), 10.0)
-    nt = a.cpu_sample_nt or (60 if not cfg.small else 200)
+    nt = min(a.cpu_sample_nt or CPU_SAMPLE_NT, cfg.NT)
     p = build_problem(vmig, N2=cfg.N2, M=cfg.M, NT=nt, h=cfg.h, tao=cfg.tao, f0=cfg.f0,
                       adaptive=False, compen=True, rec=synth.full_spread(cfg.nx, cfg.N2))
     shots = synth.surface_shots(cfg.nx, cfg.nshot, cfg.N2)
@@ -685,7 +690,7 @@ def main():
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
-        nt_s = a.cpu_sample_nt or 60
+        nt_s = min(a.cpu_sample_nt or CPU_SAMPLE_NT, cfg.NT)
         cpu = cpu_baseline(cfg, pmig, shots, seis_h.numpy(), nt_s, os.cpu_count() or 1)
 
     clocks = clk.summary(local)
