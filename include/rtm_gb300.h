@@ -119,7 +119,9 @@ int rtm_k_Rel_Compen(float *DBW2, float *DFW2, float *DBWADD, float *DFWADD, flo
  * lives in a fixed 1,048,576-value device array inside this library instead of
  * a caller DFWb buffer.  Pads with more cells are rejected (RTM_ERR_ARG).  All
  * calls share that array, so calls overlapping on the GPU race; the first call
- * on each device looks the array up (before any stream capture, please). */
+ * on each device, and the first after the device's context was re-created
+ * (cudaDeviceReset), looks the array up and should come before any stream
+ * capture. */
 int rtm_k_HybridStatic(float *DFW1, float *DFW0, float *DFW2, float *Dv, float *Dr_1, float *Dw,
                        int NZ, int NX, int N2, float taoh, float taoh2, rtm_stream_t s);
 
@@ -182,16 +184,25 @@ int rtm_mlp_grad(rtm_mlp *m, const float *x, const float *c, int n, float *grad,
 int rtm_mlp_train(rtm_mlp *m, const float *x, const float *c, int n, int epochs, int batch,
                   float lr, float *final_loss);
 int rtm_mlp_predict(rtm_mlp *m, const float *x, int n, float *c);
-/* Largest relative phase-velocity error |v_FD/v-1| of n coefficient sets
- * c[n][cstride] over kh in (0,bb] (nk samples) and angles [0,pi/4] (nth+1). */
+/* Dispersion measures: the relative phase-velocity error |v_FD/v - 1|, or
+ * the reference's own measure (h/v) |v/v_FD - 1| that its operator-length
+ * test compares with `eps` (LSMOrCon_rec_2D.cpp:321-337; h/v = tao/r). */
+#define RTM_DISP_RELATIVE 0
+#define RTM_DISP_REFERENCE 1
+/* Largest dispersion error (in the measure `metric`) of n coefficient sets
+ * c[n][cstride] over kh in (0,bb] (nk samples) and angles [0,pi/4] (nth+1);
+ * tao (the time step) is used by RTM_DISP_REFERENCE. */
 int rtm_disp_error_fp64(const double *c, int cstride, const int *M, const double *r,
-                        const double *bb, int n, int nk, int nth, double hzx, double *err);
+                        const double *bb, int n, int nk, int nth, double hzx, int metric, double tao,
+                        double *err);
 /* Coefficient table (funMandC layout) from the network with length M for
- * every needed bin; bins whose network set misses `tol` use the FP64
- * optimiser's set instead (*nfallback counts them). */
+ * every needed bin, judged by the FP64 dispersion error in the measure
+ * `metric`; for the bins whose network set misses `tol` the FP64 optimiser
+ * designs the set too and the bin keeps the lower-error set of the two
+ * (*nfallback counts the bins that keep the optimiser's). */
 int rtm_coeffs_mlp(rtm_mlp *m, const rtm_ls_settings *s, double vmin, int nvel, const int *need,
-                   int M, double tol, int *len, int *index, float *coef, int ccap, int *nc,
-                   int *nfallback, double *err_net, double *err_used);
+                   int M, double tol, int metric, int *len, int *index, float *coef, int ccap,
+                   int *nc, int *nfallback, double *err_net, double *err_used);
 
 /* ======================================================================
  * 3. Shot level.

@@ -15,6 +15,14 @@ TEST INFRASTRUCTURE ONLY.  Products:
   (only where the checkout exists; used to generate the golden fixtures).
 * ``oracle/_ref/libref_post.so`` -- DisToTimeAndTimeToDis1D.cpp and
   phase_correction_ricker_decon.cpp, likewise (the post-stack chain).
+* ``oracle/_ref/libref_gpu.so`` -- the same kernel fragment compiled by nvcc
+  for the GPU (sm_103a) under ``ref_gpu_shim.cu``, which restates the
+  reference's per-shot launch sequence: the reference's own GPU code as a
+  yardstick and parity target (built wherever nvcc is present).
+
+The reference checkout is the directory named by the RTM_REFERENCE_CHECKOUT
+environment variable or the --checkout argument (default: the checkout this
+recipe was written against).
 
 Everything is compiled with ``-ffp-contract=off`` so that neither x86-64 nor
 aarch64 fuses multiply-adds: the FP32 oracle then reproduces the reference's
@@ -29,7 +37,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-DEFAULT_CHECKOUT = "/root/reference"
+DEFAULT_CHECKOUT = os.environ.get("RTM_REFERENCE_CHECKOUT", "/root/reference")
+NVCC = os.environ.get("NVCC", "nvcc")
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
 
@@ -113,6 +122,30 @@ def build_ref(checkout: str = DEFAULT_CHECKOUT, force: bool = False) -> dict:
     return got
 
 
+def build_ref_gpu(force: bool = False) -> str:
+    """oracle/_ref/libref_gpu.so: the reference's kernels (the verbatim
+    fragment in oracle/_ref/) under ref_gpu_shim.cu, for sm_103a, with
+    nvcc's default optimisation and contraction as the reference's own build
+    line (README.md:5) uses them.  Raises when the fragment or nvcc is
+    missing."""
+    kin = os.path.join(REF_OUT, "ref_kernels.inc")
+    if not os.path.exists(kin):
+        raise RuntimeError("reference kernel fragment unavailable (no checkout, no oracle/_ref)")
+    out = os.path.join(REF_OUT, "libref_gpu.so")
+    srcs = [os.path.join(HERE, "ref_gpu_shim.cu"), kin, os.path.join(HERE, "rtm_oracle.h")]
+    if force or _stale(out, srcs):
+        _run([NVCC, "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC", "-shared",
+              "-w", "-I", REF_OUT, "-I", HERE, "-o", out + ".tmp", srcs[0]])
+        os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
-    print(build_oracle(force="--force" in sys.argv))
-    print(build_ref(force="--force" in sys.argv))
+    args = sys.argv[1:]
+    force = "--force" in args
+    checkout = DEFAULT_CHECKOUT
+    if "--checkout" in args:
+        checkout = args[args.index("--checkout") + 1]
+    print(build_oracle(force=force))
+    print(build_ref(checkout, force=force))
+    print(build_ref_gpu(force=force))

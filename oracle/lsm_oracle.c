@@ -295,16 +295,21 @@ int ls_fun_m_and_c(int nthita, int nfdmax, int nfdmin, int nvel, double tao, dou
     int NC = idx[nvel];
     if (!c) return NC;
     if (ccap < NC) return -1;
-    double *cd = (double *)malloc(sizeof(double) * (nfdmax + 1));
     double rat = tao / h, ra = 2.0 * LS_PI * fmax * tao;
-    for (int i = 0; i < nvel; ++i)
-        if (need[i] == 1) {
-            double r = (vmin + i) * rat;
-            double b = ra / r;
-            ls_coefs(cd, r, b, len[i], hzx);
-            for (int l = 0; l <= len[i]; ++l) c[l + idx[i]] = (float)cd[l];
-        }
-    free(cd);
+    /* bins are independent: spread over the host threads (same results) */
+#pragma omp parallel
+    {
+        double *cd = (double *)malloc(sizeof(double) * (nfdmax + 1));
+#pragma omp for schedule(dynamic, 8)
+        for (int i = 0; i < nvel; ++i)
+            if (need[i] == 1) {
+                double r = (vmin + i) * rat;
+                double b = ra / r;
+                ls_coefs(cd, r, b, len[i], hzx);
+                for (int l = 0; l <= len[i]; ++l) c[l + idx[i]] = (float)cd[l];
+            }
+        free(cd);
+    }
     return NC;
 }
 

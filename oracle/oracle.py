@@ -31,6 +31,7 @@ _lib = None
 _ref = None
 _refp = None
 _refh = None
+_refg = None
 
 
 def lib():
@@ -110,6 +111,38 @@ def ref():
         L.ref_ricker.argtypes = [C.c_float, C.c_float]
         _ref = L
     return _ref
+
+
+def ref_gpu():
+    """The reference's kernels on the GPU (oracle/_ref/libref_gpu.so)."""
+    global _refg
+    if _refg is None:
+        L = C.CDLL(_b.build_ref_gpu())
+        L.refgpu_migrate.restype = C.c_int
+        L.refgpu_migrate.argtypes = [C.POINTER(Params), _f32p, _f32p, _f32p, _f32p, _i32p, C.c_int,
+                                     C.c_int, _f32p, _f32p, _f32p, _f32p, C.POINTER(C.c_double)]
+        _refg = L
+    return _refg
+
+
+def ref_gpu_migrate(prob, seis):
+    """rel1, rel2 (full padded grid) and the wall-clock seconds of one shot on
+    the reference's own GPU kernels with its per-shot launch sequence
+    (kernel.cu:798-933).  Receivers other than the reference's surface line
+    are injected by the line's rule after BKAdd, as the oracle's driver does."""
+    P = make_params(prob, int(getattr(prob, "quirk", True)))
+    rel1 = np.zeros(prob.NZ * prob.NX, np.float32)
+    rel2 = np.zeros(prob.NZ * prob.NX, np.float32)
+    sec = C.c_double()
+    nvel = int(prob.nvel) if prob.adaptive else 0
+    coef = np.ascontiguousarray(prob.coef, np.float32)
+    rc = ref_gpu().refgpu_migrate(C.byref(P), prob.v.ravel(), prob.r1.ravel(), prob.w, coef,
+                                  np.ascontiguousarray(prob.index, np.int32), nvel, int(coef.size),
+                                  prob.wav, np.ascontiguousarray(seis, np.float32).ravel(), rel1,
+                                  rel2, C.byref(sec))
+    if rc != 0:
+        raise RuntimeError("reference GPU migrate failed")
+    return rel1.reshape(prob.NZ, prob.NX), rel2.reshape(prob.NZ, prob.NX), float(sec.value)
 
 
 def ref_host():

@@ -31,9 +31,12 @@ void rtm_set_last_error(const char *msg);
 
 #define RTM_DEVERR_TMA_TIMEOUT 1u
 
-// Iteration cap of every spin on an mbarrier.  try_wait suspends for a
-// hardware-chosen interval per call, so this bounds the wait to seconds.
+// Bounds of every spin on an mbarrier: at most RTM_SPIN_LIMIT polls and at
+// most RTM_WAIT_NS nanoseconds of the GPU's global timer, whichever ends the
+// wait first (try_wait suspends for a hardware-chosen interval per call, so
+// the poll count alone gives no time bound).
 #define RTM_SPIN_LIMIT (1u << 26)
+#define RTM_WAIT_NS 2000000000ull
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
 {
@@ -72,14 +75,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
     return ok != 0;
 }
 
-// Waits for phase `parity` of the barrier, at most RTM_SPIN_LIMIT polls.
-// Returns false (and ORs RTM_DEVERR_TMA_TIMEOUT into *err) when the limit is
-// hit, so a lost copy ends the kernel with an error instead of a hang.
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for phase `parity` of the barrier, at most `limit` polls and
+// RTM_WAIT_NS nanoseconds (the clock is read only once the first poll has
+// failed, and then every 64 polls).  Returns false (and ORs
+// RTM_DEVERR_TMA_TIMEOUT into *err) when a bound is hit, so a lost copy
+// ends the kernel with an error instead of a hang.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, unsigned *err,
                                                   unsigned limit = RTM_SPIN_LIMIT)
 {
-    for (unsigned it = 0; it < limit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 1; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63u) == 0 && global_ns() - t0 > RTM_WAIT_NS) break;
+    }
     atomicOr(err, RTM_DEVERR_TMA_TIMEOUT);
     return false;
 }

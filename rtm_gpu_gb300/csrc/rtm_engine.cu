@@ -77,6 +77,7 @@ struct rtm_ctx {
     // device
     float *v = nullptr, *r1 = nullptr, *w = nullptr, *ctab = nullptr;
     float4 *ctab4 = nullptr;  // adaptive table in float4 groups
+    int *blen = nullptr;      // operator length of each bin (adaptive)
     int4 *pad_meta = nullptr;
     float4 *pad_fac = nullptr;
     float *S[3] = {nullptr, nullptr, nullptr}, *R[3] = {nullptr, nullptr, nullptr};
@@ -160,6 +161,7 @@ void free_all(rtm_ctx *c)
         if (p) cudaFree(p);
     if (c->src) cudaFree(c->src);
     if (c->ctab4) cudaFree(c->ctab4);
+    if (c->blen) cudaFree(c->blen);
     for (int *q : {c->gnx, c->gxa, c->grx0, c->gitem, c->mbin, c->mbins})
         if (q) cudaFree(q);
     if (c->vs) cudaFree(c->vs);
@@ -288,6 +290,8 @@ eng::StepArgs base_step(rtm_ctx *c)
     a.nxs = c->gnx; a.rx0s = c->grx0; a.vshot = c->windowed ? 1 : 0;
     a.gbin = c->windowed ? c->mbins : c->mbin;
     a.gbin_ss = c->windowed ? c->ss : 0;
+    a.xas = c->gxa;
+    a.gsbin = c->mbin;
     return a;
 }
 
@@ -530,7 +534,7 @@ int run_phase(rtm_ctx *c, int phase, int nb, int flags)
 void model_prep(rtm_ctx *c, const float *v, long long ncell, float *vv, int *bin)
 {
     eng::k_model_prep<<<(unsigned)cdiv(ncell, 256), 256, 0, c->st>>>(
-        v, ncell, c->p.tao2, c->p.h2, c->p.vmin, c->p.dv, std::max(c->nbins, 1), vv,
+        v, ncell, c->p.tao2, c->p.h2, c->p.vmin, c->p.dv, std::max(c->nbins, 1), c->blen, vv,
         c->p.adaptive ? bin : nullptr);
 }
 
@@ -590,6 +594,9 @@ int set_batch(rtm_ctx *c, int nb, const int *src_cells, const int *xa, const int
         if (int rc = dalloc(c, &c->fac_s, (size_t)nabc * c->B)) return rc;
         if (int rc = dalloc(c, &c->mvvs, bgrid)) return rc;
         if (int rc = make_map(&c->mmaps_s.vv, c->mvvs, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ)) return rc;
+        // window-interior tiles read the survey's grid (tile_on_survey)
+        c->mmaps_s.svv = c->mmaps.vv;
+        c->mmaps_s.sbin = c->mmaps.bin;
         if (c->p.adaptive) {
             if (int rc = dalloc(c, &c->mbins, bgrid)) return rc;
             if (int rc = make_map(&c->mmaps_s.bin, reinterpret_cast<float *>(c->mbins), c->NX, c->NZ, c->B,
@@ -750,6 +757,12 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
         delete c;
         return RTM_ERR_CUDA;
     }
+    if (p->adaptive && p->nbins >= (1 << eng::BIN_BITS)) {
+        rtm_set_last_error("rtm_ctx_create: too many velocity bins");
+        free_all(c);
+        delete c;
+        return RTM_ERR_ARG;
+    }
     if (p->adaptive) {
         c->nbins = p->nbins;
         tab.assign((size_t)(c->MM + 1) * c->nbins, 0.0f);
@@ -790,9 +803,14 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
                 }
                 t4[eng::tab_index(q, b, c->nbins, c->MM)] = make_float4(g[0], g[1], g[2], g[3]);
             }
+        // each bin's operator length (unused bins: 0, their coefficients are zero)
+        std::vector<int> bl(c->nbins);
+        for (int b = 0; b < c->nbins; ++b) bl[b] = std::max(p->index[b + 1] - p->index[b] - 1, 0);
         TRY(dalloc(c, &c->ctab4, t4.size()));
+        TRY(dalloc(c, &c->blen, bl.size()));
         if (cudaMemcpy(c->ctab4, t4.data(), sizeof(float4) * t4.size(), cudaMemcpyHostToDevice) !=
-            cudaSuccess) {
+                cudaSuccess ||
+            cudaMemcpy(c->blen, bl.data(), sizeof(int) * bl.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
             rtm_set_last_error("upload failed");
             free_all(c);
             delete c;

@@ -81,10 +81,11 @@ struct ImgMaps {
 };
 
 // Per-cell model factors staged by the stencil kernels: vv = v^2 tao^2 / h^2
-// (float, kernel.cu's v*v*tao2*h2) and the velocity bin (int); one grid
-// shared by the batch or one per shot.
+// (float, kernel.cu's v*v*tao2*h2) and the bin word (int); one grid shared by
+// the batch or one per shot (vv, bin), and, for shots with their own
+// windows, the survey's grid as well (svv, sbin).
 struct ModelMaps {
-    CUtensorMap vv, bin;
+    CUtensorMap vv, bin, svv, sbin;
 };
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
@@ -120,7 +121,22 @@ struct StepArgs {
     // coefficients are gathered from it before the tile's copies land
     const int *gbin;
     long long gbin_ss;
+    // shots with their own windows: window origin (interior column of the
+    // survey) of each shot, and the survey's bins (same pitch P)
+    const int *xas;
+    const int *gsbin;
 };
+
+// Whether a tile of a windowed shot reads its model tiles from the survey's
+// grid: its columns lie inside the window's interior, where the window's
+// model equals the survey's shifted by the window origin xa (only the
+// window's own pad band is an edge extension of its own), and xa keeps the
+// survey coordinate x0 + xa a multiple of 4 floats (16 bytes, as TMA needs).
+// The survey grid is shared by every shot of the batch, so L2 serves it.
+__device__ __forceinline__ bool tile_on_survey(const StepArgs &a, int x0, int NX, int xa)
+{
+    return a.vshot && (xa & 3) == 0 && x0 >= a.N2 && x0 + TX <= NX - a.N2;
+}
 
 __device__ __forceinline__ int mirror_i(int i, int n)
 {
@@ -178,26 +194,48 @@ __host__ __device__ __forceinline__ int tab_index(int q, int bin, int nbins, int
     return RTM_TAB_BINMAJOR ? bin * tab_pitch(mmax) + q : q * nbins + bin;
 }
 
+// Per-cell bin words: the velocity bin in the low 24 bits and the bin's
+// operator length above them (k_model_prep packs them), so a cell learns both
+// from one staged int.
+constexpr int BIN_BITS = 24;
+__device__ __forceinline__ int word_bin(int bw) { return bw & ((1 << BIN_BITS) - 1); }
+__device__ __forceinline__ int word_len(int bw) { return (int)((unsigned)bw >> BIN_BITS); }
+
 // Coefficients of one cell: the velocity bin (adaptive; precomputed per cell
 // as kernel.cu:55-57 forms it) picks a column of the coefficient-major table;
-// with fixed coefficients the values are loaded once into registers (cc).
+// only the groups holding c_0..c_len of the cell's own operator length are
+// gathered and the others are zero (as the table holds them); with fixed
+// coefficients the values are loaded once into registers (cc).  Returns the
+// cell's operator length (MMAX with fixed coefficients).
 template <int MMAX, bool ADAPT>
-__device__ __forceinline__ void load_coefs(const StepArgs &a, int bin, const float *cc, float *cf)
+__device__ __forceinline__ int load_coefs(const StepArgs &a, int bw, const float *cc, float *cf)
 {
     if (!ADAPT) {
 #pragma unroll
         for (int l = 0; l <= MMAX; ++l) cf[l] = cc[l];
-        return;
+        return MMAX;
     }
     constexpr int Q = (MMAX + 4) / 4;
+    const int bin = word_bin(bw), len = word_len(bw);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const float4 g = __ldg(a.ctab4 + tab_index(q, bin, a.nbins, MMAX));
+        const float4 g = (4 * q <= len) ? __ldg(a.ctab4 + tab_index(q, bin, a.nbins, MMAX))
+                                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (4 * q + 0 <= MMAX) cf[4 * q + 0] = g.x;
         if (4 * q + 1 <= MMAX) cf[4 * q + 1] = g.y;
         if (4 * q + 2 <= MMAX) cf[4 * q + 2] = g.z;
         if (4 * q + 3 <= MMAX) cf[4 * q + 3] = g.w;
     }
+    return len;
+}
+
+// Longest operator among the warp's cells of one row: terms beyond it have
+// zero coefficients for every lane, and adding 0*x leaves a sum unchanged,
+// so the stencil loops stop there (the bits of the result do not change).
+template <int MMAX, bool ADAPT>
+__device__ __forceinline__ int warp_len(int len)
+{
+    return ADAPT ? min(__reduce_max_sync(0xffffffffu, (unsigned)len), (unsigned)MMAX) : MMAX;
 }
 
 // Spatial operator of one cell: w = k0*c0*u + sum_l c_l*((u[z-l]+u[z+l])*hzx2_1
@@ -205,11 +243,12 @@ __device__ __forceinline__ void load_coefs(const StepArgs &a, int bin, const flo
 // (centre at index C) and row the cell's row in the staged halo box.
 template <int MMAX, bool ADAPT>
 __device__ __forceinline__ float lap_cell(const float *q, int C, const float *row, const float *cf,
-                                          float k0, float hzx2_1)
+                                          float k0, float hzx2_1, int L)
 {
     float w1 = k0 * cf[0] * q[C];
 #pragma unroll
     for (int l = 1; l <= MMAX; ++l) {
+        if (l > L) break;
         const float xs = (q[C - l] + q[C + l]) * hzx2_1 + row[-l];
         w1 = fmaf(cf[l], xs + row[l], w1);
     }
@@ -259,15 +298,21 @@ __device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t
                                            const CUtensorMap &mapA, const CUtensorMap &mapS,
                                            const CUtensorMap &flatA0, const CUtensorMap &flatS0,
                                            const ModelMaps &mod, const ImgMaps &img, int x0,
-                                           int z0, int shot, int vshot, bool with_s)
+                                           int z0, int shot, int vshot, bool with_s, bool surv = false,
+                                           int xa = 0)
 {
     using S = Shape<MMAX>;
     const unsigned skip = (MODE == MODE_BWD && !with_s) ? S::BYTES + 5u * FLAT_BYTES : 0u;
     mbar_arrive_expect_tx(bar, stage_tx_bytes<MMAX, MODE, ADAPT>() - skip);
     tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
     tma_load_3d(st.fA0, &flatA0, x0, z0, shot, bar);
-    tma_load_3d(st.fV, &mod.vv, x0, z0, vshot ? shot : 0, bar);
-    if (ADAPT) tma_load_3d(st.fB, &mod.bin, x0, z0, vshot ? shot : 0, bar);
+    if (surv) {
+        tma_load_3d(st.fV, &mod.svv, x0 + xa, z0, 0, bar);
+        if (ADAPT) tma_load_3d(st.fB, &mod.sbin, x0 + xa, z0, 0, bar);
+    } else {
+        tma_load_3d(st.fV, &mod.vv, x0, z0, vshot ? shot : 0, bar);
+        if (ADAPT) tma_load_3d(st.fB, &mod.bin, x0, z0, vshot ? shot : 0, bar);
+    }
     if (MODE == MODE_BWD && with_s) {
         tma_load_3d(st.tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, bar);
         tma_load_3d(st.fS0, &flatS0, x0, z0, shot, bar);
@@ -289,16 +334,17 @@ __device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t
 // overlaps the copies instead of stalling the first rows).
 template <int MMAX, bool ADAPT, int PRE>
 __device__ __forceinline__ void pre_gather(const StepArgs &a, const float *cc, int x0, int z0, int shot,
-                                           int NX, float (&cf)[PRE > 0 ? PRE : 1][MMAX + 1])
+                                           int NX, float (&cf)[PRE > 0 ? PRE : 1][MMAX + 1],
+                                           int (&len)[PRE > 0 ? PRE : 1], bool surv, int xa)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int zw = z0 + (warp / WX) * RW, gx = x0 + (warp % WX) * 32 + lane;
-    const int *gb = a.gbin ? a.gbin + shot * a.gbin_ss : nullptr;
+    const int *gb = surv ? a.gsbin + xa : (a.gbin ? a.gbin + shot * a.gbin_ss : nullptr);
 #pragma unroll
     for (int r = 0; r < PRE; ++r) {
         int b = 0;
         if (ADAPT && gb && zw + r < a.NZ && gx < NX) b = __ldg(gb + (long)(zw + r) * a.P + gx);
-        load_coefs<MMAX, ADAPT>(a, b, cc, cf[r]);
+        len[r] = load_coefs<MMAX, ADAPT>(a, b, cc, cf[r]);
     }
 }
 
@@ -306,7 +352,7 @@ template <int MMAX, bool ADAPT, int MODE, int PF, int PRE>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX, MODE> &st,
                                              const float *cc, int x0, int z0, int shot, int NX,
                                              const float (&cpre)[PRE > 0 ? PRE : 1][MMAX + 1],
-                                             int src, int rx0)
+                                             const int (&lpre)[PRE > 0 ? PRE : 1], int src, int rx0)
 {
     using S = Shape<MMAX>;
     constexpr int QN = 2 * MMAX + 1;
@@ -337,12 +383,15 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     // a gather depends on the staged velocity and usually misses L1, so
     // issuing it early hides its latency behind the rows in between.
     float cfr[RW][MMAX + 1];
+    int lr[RW];  // operator length of the lane's cell in each row
 #pragma unroll
-    for (int i = 0; i < PRE; ++i)
+    for (int i = 0; i < PRE; ++i) {
+        lr[i] = lpre[i];
 #pragma unroll
         for (int l = 0; l <= MMAX; ++l) cfr[i][l] = cpre[i][l];
+    }
 #pragma unroll
-    for (int i = PRE; i < PF; ++i) load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + i * TX] : 0, cc, cfr[i]);
+    for (int i = PRE; i < PF; ++i) lr[i] = load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + i * TX] : 0, cc, cfr[i]);
 
     if (MODE == MODE_FWD) {
         // two rows per iteration: two independent accumulation chains
@@ -354,7 +403,8 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #pragma unroll
             for (int h = 0; h < 2; ++h)
                 if (i + h + PF < RW && i + h + PF >= PRE)
-                    load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + h + PF) * TX] : 0, cc, cfr[i + h + PF]);
+                    lr[i + h + PF] =
+                        load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + h + PF) * TX] : 0, cc, cfr[i + h + PF]);
             q[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
             q[QN] = tA[(rbase + i + QN) * S::BW + cx];
 #pragma unroll
@@ -364,7 +414,8 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
                 const int t = fr + (i + h) * TX;
                 const float *cf = cfr[i + h];
                 const float *row = tA + (rbase + i + h + MMAX) * S::BW + cx;
-                const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cf, a.k0, a.hzx2_1);
+                const int L = warp_len<MMAX, ADAPT>(lr[i + h]);
+                const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cf, a.k0, a.hzx2_1, L);
                 float val = fmaf(fV[t], w1, 2.0f * q[MMAX + h] - fA0[t]);
                 if (i + h == src_row) val += a.wavelet;
                 const long long g = g0 + (long)(i + h) * a.P;
@@ -402,7 +453,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #pragma unroll
     for (int i = 0; i < RW; ++i) {
         if (i + PF < RW && i + PF >= PRE)
-            load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + PF) * TX] : 0, cc, cfr[i + PF]);
+            lr[i + PF] = load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + (i + PF) * TX] : 0, cc, cfr[i + PF]);
         qr[QN - 1] = tA[(rbase + i + QN - 1) * S::BW + cx];
         if (rows_s) qs[QN - 1] = tS[(rbase + i + QN - 1) * S::BW + cx];
         const int z = zw + i;
@@ -415,8 +466,10 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
             const float c0 = cf[0];
             float wr = a.k0 * c0 * qr[MMAX];
             float ws = a.k0 * c0 * qs[MMAX];
+            const int L = warp_len<MMAX, ADAPT>(lr[i]);
 #pragma unroll
             for (int l = 1; l <= MMAX; ++l) {
+                if (l > L) break;
                 const float cl = cf[l];
                 wr = fmaf(cl, (qr[MMAX - l] + qr[MMAX + l]) * a.hzx2_1 + rowR[-l] + rowR[l], wr);
                 if (rows_s)
@@ -507,17 +560,19 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     const Stage<MMAX, MODE> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
-    // the shot's width: a load only when shots have their own windows, so
-    // that nothing delays the tile's copies otherwise
+    // the shot's width and window origin: loads only when shots have their
+    // own windows, so that nothing delays the tile's copies otherwise
     const int NX = a.vshot ? a.nxs[shot] : a.NX;
+    const int xa = a.vshot ? a.xas[shot] : 0;
     if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
+    const bool surv = tile_on_survey(a, x0, NX, xa);
 
     const bool with_s = tile_has_interior_rows(z0, a.NZ, a.N2);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
         issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
-                                      with_s);
+                                      with_s, surv, xa);
     }
     // fixed coefficients: once per thread, while the copies are in flight;
     // the first rows' adaptive coefficients likewise (issued by every thread
@@ -529,7 +584,8 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     // coefficients would not fit its registers)
     constexpr int PRE = !ADAPT ? 0 : (MODE == MODE_BWD ? (MMAX <= 8 ? RTM_BWD_PRE : 2) : RTM_FWD_PRE);
     float cpre[PRE > 0 ? PRE : 1][MMAX + 1];
-    pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre);
+    int lpre[PRE > 0 ? PRE : 1];
+    pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre, lpre, surv, xa);
     const int src = __ldg(a.src + shot), rx0 = MODE == MODE_BWD ? __ldg(a.rx0s + shot) : 0;
     __syncthreads();  // the barrier is initialised before any thread waits on it
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
@@ -548,7 +604,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
         return;
     }
-    compute_tile<MMAX, ADAPT, MODE, PF, PRE>(a, st, cc, x0, z0, shot, NX, cpre, src, rx0);
+    compute_tile<MMAX, ADAPT, MODE, PF, PRE>(a, st, cc, x0, z0, shot, NX, cpre, lpre, src, rx0);
 }
 
 // Forward step with two columns per lane (kernel form RTM_KERNEL_X2): the
@@ -560,12 +616,13 @@ constexpr int X2_THREADS = 128;
 
 template <int MMAX, bool ADAPT>
 __device__ __forceinline__ float lap_regs(const float *q, int C, const float *xv, int o, const float *cf,
-                                          float k0, float hzx2_1)
+                                          float k0, float hzx2_1, int L)
 {
     // xv[o + j] is the row's value at column (cell - MMAX + j)
     float w1 = k0 * cf[0] * q[C];
 #pragma unroll
     for (int l = 1; l <= MMAX; ++l) {
+        if (l > L) break;
         const float xs = (q[C - l] + q[C + l]) * hzx2_1 + xv[o + MMAX - l];
         w1 = fmaf(cf[l], xs + xv[o + MMAX + l], w1);
     }
@@ -590,12 +647,14 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE_FWD>());
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
     const int NX = a.vshot ? a.nxs[shot] : a.NX;
+    const int xa = a.vshot ? a.xas[shot] : 0;
     if (x0 >= NX) return;
+    const bool surv = tile_on_survey(a, x0, NX, xa);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
         issue_tile<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot,
-                                          a.vshot, false);
+                                          a.vshot, false, surv, xa);
     }
     float cc[MMAX + 1];
 #pragma unroll
@@ -608,8 +667,9 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
     // coefficients of the first row pair, gathered from the global bins
     // while the tile's copies are in flight
     float cpa[2][MMAX + 1], cpb[2][MMAX + 1];
+    int lpa[2], lpb[2];
     {
-        const int *gb = (ADAPT && a.gbin) ? a.gbin + shot * a.gbin_ss : nullptr;
+        const int *gb = !ADAPT ? nullptr : (surv ? a.gsbin + xa : (a.gbin ? a.gbin + shot * a.gbin_ss : nullptr));
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
             int ba = 0, bb = 0;
@@ -618,8 +678,8 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
                 if (gx < NX) ba = __ldg(rowb);
                 if (gx + 1 < NX) bb = __ldg(rowb + 1);
             }
-            load_coefs<MMAX, ADAPT>(a, ba, cc, cpa[r]);
-            load_coefs<MMAX, ADAPT>(a, bb, cc, cpb[r]);
+            lpa[r] = load_coefs<MMAX, ADAPT>(a, ba, cc, cpa[r]);
+            lpb[r] = load_coefs<MMAX, ADAPT>(a, bb, cc, cpb[r]);
         }
     }
     const int src = __ldg(a.src + shot);
@@ -670,15 +730,11 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
             if (z >= NZ) continue;
             const int t = fr + (i + h) * TX;
             const float *row = tA + (rbase + i + h + MMAX) * S::BW + cx - MMAX;  // even offset
-            float xv[NXV];
-#pragma unroll
-            for (int j = 0; j < NXV; j += 2) {
-                const float2 v = *reinterpret_cast<const float2 *>(row + j);
-                xv[j] = v.x;
-                xv[j + 1] = v.y;
-            }
             float cfa[MMAX + 1], cfb[MMAX + 1];
+            int la, lb;
             if (i == 0) {
+                la = lpa[h];
+                lb = lpb[h];
 #pragma unroll
                 for (int l = 0; l <= MMAX; ++l) {
                     cfa[l] = cpa[h][l];
@@ -686,13 +742,26 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
                 }
             } else {
                 const int2 bins = ADAPT ? *reinterpret_cast<const int2 *>(fB + t) : make_int2(0, 0);
-                load_coefs<MMAX, ADAPT>(a, bins.x, cc, cfa);
-                load_coefs<MMAX, ADAPT>(a, bins.y, cc, cfb);
+                la = load_coefs<MMAX, ADAPT>(a, bins.x, cc, cfa);
+                lb = load_coefs<MMAX, ADAPT>(a, bins.y, cc, cfb);
+            }
+            const int L = warp_len<MMAX, ADAPT>(max(la, lb));
+            // x values the warp's operators reach: columns MMAX-L .. MMAX+1+L of xv
+            float xv[NXV];
+#pragma unroll
+            for (int j = 0; j < NXV; j += 2) {
+                if (j + 1 < MMAX - L || j > MMAX + 1 + L) {
+                    xv[j] = xv[j + 1] = 0.0f;
+                    continue;
+                }
+                const float2 v = *reinterpret_cast<const float2 *>(row + j);
+                xv[j] = v.x;
+                xv[j + 1] = v.y;
             }
             const float2 vv = *reinterpret_cast<const float2 *>(fV + t);
             const float2 u0 = *reinterpret_cast<const float2 *>(fA0 + t);
-            const float wa = lap_regs<MMAX, ADAPT>(qa, MMAX + h, xv, 0, cfa, a.k0, a.hzx2_1);
-            const float wb = lap_regs<MMAX, ADAPT>(qb, MMAX + h, xv, 1, cfb, a.k0, a.hzx2_1);
+            const float wa = lap_regs<MMAX, ADAPT>(qa, MMAX + h, xv, 0, cfa, a.k0, a.hzx2_1, L);
+            const float wb = lap_regs<MMAX, ADAPT>(qb, MMAX + h, xv, 1, cfb, a.k0, a.hzx2_1, L);
             float va = fmaf(vv.x, wa, 2.0f * qa[MMAX + h] - u0.x);
             float vb = fmaf(vv.y, wb, 2.0f * qb[MMAX + h] - u0.y);
             if (i + h == src_row0) va += a.wavelet;
@@ -806,8 +875,9 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
         }
         phase ^= 1u << s;
         const float nopre[1][MMAX + 1] = {};
-        compute_tile<MMAX, ADAPT, MODE, PF, 0>(a, cur, cc, x0, z0, shot, NX, nopre, __ldg(a.src + shot),
-                                               __ldg(a.rx0s + shot));
+        const int nolen[1] = {0};
+        compute_tile<MMAX, ADAPT, MODE, PF, 0>(a, cur, cc, x0, z0, shot, NX, nopre, nolen,
+                                               __ldg(a.src + shot), __ldg(a.rx0s + shot));
         __syncthreads();  // every thread is done with this stage before it is reloaded
         shot = nshot; x0 = nx0; z0 = nz0;
     }
@@ -1119,16 +1189,14 @@ __global__ void k_window_model(const float *vg, const float *r1g, int Pg, const 
     r1s[o] = r1g[(z >= N2 && z < NZ - N2) ? gi : gz];
 }
 
-// Pad tables of each shot's grid (the device form of the table rtm_ctx_create
-// builds for a single grid): classification, inward directions, ring slot and
-// the model factors, from the shot's own padded model.
 // Per-cell model factors of nshot grids [shot][NZ][P]: vv = v*v*tao2*h2 in
-// the reference's float order, and the velocity bin int((v-vmin)/dv + 0.5)
-// with the 0.5 added in double as the reference's kernels do
-// (kernel.cu:56), clamped to the table.
+// the reference's float order, and the bin word: the velocity bin
+// int((v-vmin)/dv + 0.5), with the 0.5 added in double as the reference's
+// kernels do (kernel.cu:56) and clamped to the table, packed with that bin's
+// operator length blen[bin] (word_bin / word_len).
 __global__ void k_model_prep(const float *__restrict__ v, long long ncell, float tao2, float h2,
-                             float vmin, float dv, int nbins, float *__restrict__ vv,
-                             int *__restrict__ bin)
+                             float vmin, float dv, int nbins, const int *__restrict__ blen,
+                             float *__restrict__ vv, int *__restrict__ bin)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ncell) return;
@@ -1136,10 +1204,14 @@ __global__ void k_model_prep(const float *__restrict__ v, long long ncell, float
     vv[i] = __fmul_rn(__fmul_rn(__fmul_rn(x, x), tao2), h2);
     if (bin) {
         const float q = __fdiv_rn(__fsub_rn(x, vmin), dv);
-        const int b = (int)((double)q + 0.5);
-        bin[i] = min(max(b, 0), nbins - 1);
+        const int b = min(max((int)((double)q + 0.5), 0), nbins - 1);
+        bin[i] = b | (blen[b] << BIN_BITS);
     }
 }
+
+// Pad tables of each shot's grid (the device form of the table rtm_ctx_create
+// builds for a single grid): classification, inward directions, ring slot and
+// the model factors, from the shot's own padded model.
 
 __global__ void k_pad_tables(const float *vs, const float *r1s, const float *w, const int *nxs,
                              long long ss, long long tab_ss, int NZ, int P, int N2, int M,

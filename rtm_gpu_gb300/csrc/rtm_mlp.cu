@@ -201,7 +201,8 @@ __global__ void k_gather(const float *x, const float *t, const int *idx, int n, 
 //                                        + sin^2(l hzx kh sin th/2)/hzx^2) ) )
 // One block per set.
 __global__ void k_disp_err(const double *c, int cstride, const int *M, const double *r,
-                           const double *bb, int nk, int nth, double hzx, double *err)
+                           const double *bb, int nk, int nth, double hzx, int metric, double tao,
+                           double *err)
 {
     const int s = blockIdx.x;
     const int m = M[s];
@@ -217,7 +218,14 @@ __global__ void k_disp_err(const double *c, int cstride, const int *M, const dou
             mid += c[(long)s * cstride + l] * (s1 * s1 / (hzx * hzx) + s2 * s2);
         }
         const double arg = rr * sqrt(fmax(mid, 0.0));
-        const double e = (arg <= 1.0) ? fabs(2.0 / (rr * kh) * asin(arg) - 1.0) : 1.0;
+        double e;
+        if (arg > 1.0 || !(arg > 0.0)) {
+            e = 1.0;  // no real phase velocity: the operator is unstable here
+        } else {
+            const double ratio = 2.0 / (rr * kh) * asin(arg);  // v_FD / v
+            // metric 1: the reference's measure (h/v) |v/v_FD - 1|, h/v = tao/r
+            e = metric ? fabs(1.0 / ratio - 1.0) * (tao / rr) : fabs(ratio - 1.0);
+        }
         worst = fmax(worst, e);
     }
     __shared__ double red[256];
@@ -452,12 +460,17 @@ int rtm_mlp_predict(rtm_mlp *m, const float *x, int n, float *c)
     return RTM_OK;
 }
 
-// Largest relative phase-velocity error of n coefficient sets c[n][cstride]
-// (c_0..c_M in FP64) at Courant numbers r and band limits bb.
+// Largest phase-velocity error of n coefficient sets c[n][cstride] (c_0..c_M
+// in FP64) at Courant numbers r and band limits bb, in the measure `metric`
+// (RTM_DISP_RELATIVE or RTM_DISP_REFERENCE; tao is the time step of the
+// latter's h/v = tao/r).
 int rtm_disp_error_fp64(const double *c, int cstride, const int *M, const double *r,
-                        const double *bb, int n, int nk, int nth, double hzx, double *err)
+                        const double *bb, int n, int nk, int nth, double hzx, int metric, double tao,
+                        double *err)
 {
-    if (!c || !M || !r || !bb || !err || n < 1 || nk < 1 || nth < 1) return RTM_ERR_ARG;
+    if (!c || !M || !r || !bb || !err || n < 1 || nk < 1 || nth < 1 ||
+        (metric != RTM_DISP_RELATIVE && metric != RTM_DISP_REFERENCE) || (metric && !(tao > 0)))
+        return RTM_ERR_ARG;
     DBuf<double> dc, dr, dbb, de;
     DBuf<int> dm;
     int rc;
@@ -468,7 +481,7 @@ int rtm_disp_error_fp64(const double *c, int cstride, const int *M, const double
     RTM_CUDA_TRY(cudaMemcpy(dr.p, r, sizeof(double) * n, cudaMemcpyHostToDevice));
     RTM_CUDA_TRY(cudaMemcpy(dbb.p, bb, sizeof(double) * n, cudaMemcpyHostToDevice));
     RTM_CUDA_TRY(cudaMemcpy(dm.p, M, sizeof(int) * n, cudaMemcpyHostToDevice));
-    k_disp_err<<<n, 256>>>(dc.p, cstride, dm.p, dr.p, dbb.p, nk, nth, hzx, de.p);
+    k_disp_err<<<n, 256>>>(dc.p, cstride, dm.p, dr.p, dbb.p, nk, nth, hzx, metric, tao, de.p);
     RTM_LAUNCH_CHECK();
     RTM_CUDA_TRY(cudaMemcpy(err, de.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
     return RTM_OK;
@@ -480,15 +493,20 @@ int rtm_ls_coefs_fp64(const double *r, const double *bb, const int *M, int n, do
 // Coefficient table (the layout of funMandC, LSMOrCon_rec_2D.cpp:45-66) from
 // the network: every needed bin i (velocity vmin + i, band limit
 // bb = 2 pi fmax tao / r as funMandC designs it) gets operator length M and
-// the network's coefficients when their largest relative phase-velocity
-// error is <= tol, otherwise the FP64 optimiser's (counted in *nfallback).
-// err_net[nvel] / err_used[nvel] (optional) receive the errors of the
-// network's set and of the set kept (-1 for bins not needed).
+// the network's coefficients when their largest phase-velocity error (in the
+// measure `metric`) is <= tol.  For the other bins the FP64 optimiser designs
+// the set too, and the bin keeps whichever of the two sets has the lower
+// error (*nfallback counts the bins that keep the optimiser's), so no bin's
+// error is above the network's or the optimiser's.  err_net[nvel] /
+// err_used[nvel] (optional) receive the errors of the network's set and of
+// the set kept (-1 for bins not needed).
 int rtm_coeffs_mlp(rtm_mlp *m, const rtm_ls_settings *s, double vmin, int nvel, const int *need,
-                   int M, double tol, int *len, int *index, float *coef, int ccap, int *nc,
-                   int *nfallback, double *err_net, double *err_used)
+                   int M, double tol, int metric, int *len, int *index, float *coef, int ccap,
+                   int *nc, int *nfallback, double *err_net, double *err_used)
 {
-    if (!m || !s || nvel < 1 || !need || !len || !index || !nc || M < 1 || M > NO) return RTM_ERR_ARG;
+    if (!m || !s || nvel < 1 || !need || !len || !index || !nc || M < 1 || M > NO ||
+        (metric != RTM_DISP_RELATIVE && metric != RTM_DISP_REFERENCE))
+        return RTM_ERR_ARG;
     index[0] = 0;
     for (int i = 0; i < nvel; ++i) {
         len[i] = need[i] ? M : -1;
@@ -534,12 +552,13 @@ int rtm_coeffs_mlp(rtm_mlp *m, const rtm_ls_settings *s, double vmin, int nvel, 
     const int nk = std::max(8, (int)(s->fmax / s->df));
     std::vector<double> err(nb);
     if (int rc = rtm_disp_error_fp64(cd.data(), CS, mm.data(), rr.data(), bbv.data(), nb, nk, 32,
-                                     s->hzx, err.data()))
+                                     s->hzx, metric, s->tao, err.data()))
         return rc;
     std::vector<int> fb;
     for (int q = 0; q < nb; ++q)
         if (!(err[q] <= tol)) fb.push_back(q);
     std::vector<double> used_err(err);
+    int nopt = 0;
     if (!fb.empty()) {
         std::vector<double> fr, fbb, fc((size_t)fb.size() * CS);
         std::vector<int> fm(fb.size(), M);
@@ -551,14 +570,17 @@ int rtm_coeffs_mlp(rtm_mlp *m, const rtm_ls_settings *s, double vmin, int nvel, 
             return rc;
         std::vector<double> ferr(fb.size());
         if (int rc = rtm_disp_error_fp64(fc.data(), CS, fm.data(), fr.data(), fbb.data(), (int)fb.size(),
-                                         nk, 32, s->hzx, ferr.data()))
+                                         nk, 32, s->hzx, metric, s->tao, ferr.data()))
             return rc;
         for (size_t k = 0; k < fb.size(); ++k) {
+            // the lower-error set of the two (a NaN error never wins)
+            if (!(ferr[k] < err[fb[k]]) && err[fb[k]] == err[fb[k]]) continue;
             std::copy(fc.begin() + k * CS, fc.begin() + (k + 1) * CS, cd.begin() + (size_t)fb[k] * CS);
             used_err[fb[k]] = ferr[k];
+            ++nopt;
         }
     }
-    if (nfallback) *nfallback = (int)fb.size();
+    if (nfallback) *nfallback = nopt;
     for (int q = 0; q < nb; ++q) {
         const int i = bins[q];
         for (int l = 0; l <= M; ++l) coef[index[i] + l] = (float)cd[(size_t)q * CS + l];

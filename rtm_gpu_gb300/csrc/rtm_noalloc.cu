@@ -23,8 +23,13 @@
 // Set-up: host code cannot use the array's name as a device address (it is a
 // host-side stand-in), so the first call on each device looks the device
 // address up with cudaGetSymbolAddress while that device is current and
-// caches it.  That first call on a device should therefore come before any
-// stream capture.
+// caches it together with the unique id of the device's current context.
+// A call that finds a different context (the device was reset and its
+// context re-created, which can move the array) looks the address up again.
+// The first call on a device, and the first after a reset, should therefore
+// come before any stream capture.
+#include <cudaTypedefs.h>
+
 #include <mutex>
 
 #include "rtm_common.cuh"
@@ -38,6 +43,40 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 float *g_scratch_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};  // context id the address belongs to
+
+// Unique id of the calling thread's current context (cuCtxGetId: unique for
+// the life of the process, so a re-created context never matches an old id).
+// Returns RTM_OK, 1 when no context is current yet, or an error code.
+int current_context_id(unsigned long long *id)
+{
+    static PFN_cuCtxGetCurrent_v4000 get_cur = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    if (!get_cur || !get_id) {
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1, r2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &r1) !=
+                cudaSuccess || r1 != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2) !=
+                cudaSuccess || r2 != cudaDriverEntryPointSuccess) {
+            rtm_set_last_error("rtm_k_HybridStatic: driver context queries unavailable");
+            return RTM_ERR_CUDA;
+        }
+        get_cur = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(q);
+    }
+    CUcontext ctx = nullptr;
+    if (get_cur(&ctx) != CUDA_SUCCESS) {
+        rtm_set_last_error("rtm_k_HybridStatic: cuCtxGetCurrent failed");
+        return RTM_ERR_CUDA;
+    }
+    if (!ctx) return 1;
+    if (get_id(ctx, id) != CUDA_SUCCESS) {
+        rtm_set_last_error("rtm_k_HybridStatic: cuCtxGetId failed");
+        return RTM_ERR_CUDA;
+    }
+    return RTM_OK;
+}
 
 int scratch_for_current_device(float **out)
 {
@@ -47,15 +86,21 @@ int scratch_for_current_device(float **out)
         rtm_set_last_error("rtm_k_HybridStatic: device ordinal out of range");
         return RTM_ERR_ARG;
     }
+    unsigned long long ctx = 0;
+    const int have = current_context_id(&ctx);
+    if (have < 0) return have;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (have != RTM_OK || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
+        // (the lookup also makes the device's primary context current)
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_pad_scratch);
         if (e != cudaSuccess) {
             rtm_set_last_error(cudaGetErrorString(e));
             return RTM_ERR_CUDA;
         }
+        if (int rc = current_context_id(&ctx)) return rc < 0 ? rc : RTM_ERR_CUDA;
         g_scratch_ptr[dev] = static_cast<float *>(p);
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_ptr[dev];
     return RTM_OK;

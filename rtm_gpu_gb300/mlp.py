@@ -16,6 +16,9 @@ from . import capi, coeffs
 from .problem import f32
 
 NI, NO = 3, 16
+# dispersion measures (include/rtm_gb300.h): |v_FD/v - 1|, and the
+# reference's (h/v) |v/v_FD - 1| that its operator-length test compares with eps
+DISP_RELATIVE, DISP_REFERENCE = 0, 1
 
 
 def _bind(L):
@@ -34,9 +37,9 @@ def _bind(L):
     L.rtm_mlp_predict.argtypes = [vp, capi.fp, C.c_int, capi.fp]
     dp = C.POINTER(C.c_double)
     L.rtm_disp_error_fp64.argtypes = [dp, C.c_int, capi.ip, dp, dp, C.c_int, C.c_int, C.c_int,
-                                      C.c_double, dp]
+                                      C.c_double, C.c_int, C.c_double, dp]
     L.rtm_coeffs_mlp.argtypes = [vp, C.POINTER(coeffs.LsSettings), C.c_double, C.c_int, capi.ip,
-                                 C.c_int, C.c_double, capi.ip, capi.ip, vp, C.c_int,
+                                 C.c_int, C.c_double, C.c_int, capi.ip, capi.ip, vp, C.c_int,
                                  C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]
     L._mlp_bound = True
 
@@ -64,8 +67,10 @@ def fit_norm(x, c=None):
     return [a.astype(np.float32) for a in (in_mean, in_scale, out_mean, out_scale)]
 
 
-def dispersion_error(c, M, r, bb, nk=64, nth=32, hzx=1.0):
-    """Largest |v_FD/v - 1| of coefficient sets c[n, >=M+1] (FP64, GPU)."""
+def dispersion_error(c, M, r, bb, nk=64, nth=32, hzx=1.0, metric=DISP_RELATIVE, tao=0.0):
+    """Largest dispersion error of coefficient sets c[n, >=M+1] (FP64, GPU):
+    |v_FD/v - 1| (DISP_RELATIVE) or the reference's (h/v)|v/v_FD - 1| with
+    h/v = tao/r (DISP_REFERENCE)."""
     L = capi.lib()
     _bind(L)
     c = np.ascontiguousarray(c, np.float64)
@@ -76,7 +81,8 @@ def dispersion_error(c, M, r, bb, nk=64, nth=32, hzx=1.0):
     dp = C.POINTER(C.c_double)
     capi.check(L.rtm_disp_error_fp64(c.ctypes.data_as(dp), c.shape[1], capi.iptr(M),
                                      r.ctypes.data_as(dp), bb.ctypes.data_as(dp), len(r), nk, nth,
-                                     hzx, err.ctypes.data_as(dp)), "disp_error_fp64")
+                                     hzx, int(metric), float(tao), err.ctypes.data_as(dp)),
+               "disp_error_fp64")
     return err
 
 
@@ -147,9 +153,11 @@ class Mlp:
         return c
 
     def table(self, *, M, tol, tao, h, fmax, df=1.0, nthita=1000, eps=1e-5, hzx=1.0, vmin, nvel,
-              need):
+              need, metric=DISP_REFERENCE):
         """(length, index, coef, info) of a coefficient table built with the
-        network (length M everywhere), optimiser fallback above `tol`."""
+        network (length M everywhere), judged by the FP64 dispersion error in
+        the measure `metric`; bins whose network set misses `tol` keep the
+        lower-error set of the network's and the optimiser's."""
         L = capi.lib()
         s = coeffs.LsSettings(int(nthita), int(M), int(M), f32(tao), f32(h), f32(df), f32(eps),
                               f32(fmax), float(hzx))
@@ -161,12 +169,12 @@ class Mlp:
         en = np.zeros(nvel, np.float64)
         eu = np.zeros(nvel, np.float64)
         capi.check(L.rtm_coeffs_mlp(self._h, C.byref(s), float(vmin), nvel, capi.iptr(need), M, tol,
-                                    capi.iptr(length), capi.iptr(index), None, 0, C.byref(nc),
-                                    C.byref(nfb), None, None), "coeffs_mlp")
+                                    int(metric), capi.iptr(length), capi.iptr(index), None, 0,
+                                    C.byref(nc), C.byref(nfb), None, None), "coeffs_mlp")
         coef = np.zeros(nc.value, np.float32)
         t0 = time.perf_counter()
         capi.check(L.rtm_coeffs_mlp(self._h, C.byref(s), float(vmin), nvel, capi.iptr(need), M, tol,
-                                    capi.iptr(length), capi.iptr(index),
+                                    int(metric), capi.iptr(length), capi.iptr(index),
                                     C.c_void_p(coef.ctypes.data), nc.value, C.byref(nc),
                                     C.byref(nfb), en.ctypes.data_as(dp), eu.ctypes.data_as(dp)),
                    "coeffs_mlp")

@@ -167,7 +167,7 @@ def test_migrate_stack_matches_oracle(product_lib, cuda_ok, vhi):
     assert rel_l2(gu, np.stack(ups)) < TOL
     assert rel_l2(gd, np.stack(downs)) < TOL
     assert rel_l2(ill, ill_o) < TOL
-    assert rel_l2(img, img_o) < 10 * TOL
+    assert rel_l2(img, img_o) < TOL
 
 
 def test_bounded_wait_gives_up_and_context_survives(product_lib, cuda_ok):

@@ -43,37 +43,55 @@ def test_training_reduces_loss(product_lib, cuda_ok, data):
 
 
 def test_table_gain_over_optimiser(product_lib, cuda_ok):
-    """A table for 600 velocity bins at M=8 built with a network trained for
-    the survey's range of (r, kh), the optimiser as fallback, against the
-    optimiser for every bin.  Every bin stays within max(tol, optimiser's own
-    error); the network must carry some bins."""
-    tao, h, fmax = 0.001, 10.0, 45.0
-    vmin, nvel = 2000.0, 600
-    r_lo, r_hi = vmin * tao / h, (vmin + nvel) * tao / h
+    """The C5 band (v 1500-6000 m/s, h=10 m, tao=1 ms, fmax=50 Hz; 4501 bins of
+    1 m/s) at operator length 8: a table built with a network trained on 200k
+    optimiser samples of the band, judged in the reference's own dispersion
+    measure (h/v)|v/v_FD - 1| at tolerance 1e-4, against the FP64 optimiser
+    for every bin.
+
+    What the network gains: at this length the least-squares normal
+    equations are ill-conditioned where the band is narrow, and the
+    optimiser's worst bins miss the band by a wide margin; the network's sets
+    are smooth in (r, kh) and the table's worst relative phase-velocity error
+    is several times lower than the optimiser table's.  No bin keeps a set
+    worse than the better of the two."""
+    tao, h, fmax, M = 0.001, 10.0, 50.0, 8
+    vmin, nvel = 1500.0, 4501
+    r_lo, r_hi = vmin * tao / h, (vmin + nvel - 1) * tao / h
     kh = lambda v: 2.0 * np.pi * fmax * h / v
-    net, loss = mlp.train_default(n=20000, epochs=150, seed=2, batch=512, lr=3e-3,
+    t0 = time.perf_counter()
+    net, loss = mlp.train_default(n=200_000, epochs=30, seed=2, batch=512, lr=3e-3,
                                   r_range=(r_lo * 0.98, r_hi * 1.02),
-                                  kh_range=(kh(vmin + nvel) * 0.98, kh(vmin) * 1.02),
-                                  m_range=(8, 8))
+                                  kh_range=(kh(vmin + nvel - 1) * 0.98, kh(vmin) * 1.02),
+                                  m_range=(M, M))
+    t_train = time.perf_counter() - t0
     need = np.ones(nvel, np.int32)
-    tol = 3e-3
-    length, index, coef, info = net.table(M=8, tol=tol, tao=tao, h=h, fmax=fmax, vmin=vmin,
-                                          nvel=nvel, need=need)
+    tol = 1e-4
+    length, index, coef, info = net.table(M=M, tol=tol, tao=tao, h=h, fmax=fmax, vmin=vmin,
+                                          nvel=nvel, need=need, metric=mlp.DISP_REFERENCE)
     r = (vmin + np.arange(nvel)) * float(f32(tao)) / float(f32(h))
     bb = 2.0 * 3.1415926535898 * float(f32(fmax)) * float(f32(tao)) / r
     t0 = time.perf_counter()
-    copt = coeffs.ls_coefs(r, bb, 8)
+    copt = coeffs.ls_coefs(r, bb, M)
     t_opt = time.perf_counter() - t0
-    err_opt = mlp.dispersion_error(copt, np.full(nvel, 8), r, bb)
-    taylor = np.tile(np.asarray(prep_taylor(8), np.float64), (nvel, 1))
-    err_tay = mlp.dispersion_error(taylor, np.full(nvel, 8), r, bb)
+    nk = int(fmax)
+    ref_opt = mlp.dispersion_error(copt, np.full(nvel, M), r, bb, nk=nk, metric=mlp.DISP_REFERENCE,
+                                   tao=float(f32(tao)))
+    rel_opt = mlp.dispersion_error(copt, np.full(nvel, M), r, bb, nk=nk)
+    tab = np.zeros((nvel, M + 1), np.float64)
+    for i in range(nvel):
+        tab[i] = coef[index[i]:index[i] + M + 1]
+    rel_tab = mlp.dispersion_error(tab, np.full(nvel, M), r, bb, nk=nk)
     used, en = info["err_used"], info["err_net"]
-    print("training loss %.3g; network error quantiles (10/50/90/max) %s; Taylor max %.2e"
-          % (loss, " ".join("%.2e" % q for q in np.quantile(en, [0.1, 0.5, 0.9, 1.0])),
-             err_tay.max()))
-    print("network table: %.3f s, %d/%d bins from the network, max error %.2e "
-          "(optimiser alone: %.3f s, max error %.2e)"
-          % (info["seconds"], nvel - info["fallback"], nvel, used.max(), t_opt, err_opt.max()))
-    assert np.all(used <= np.maximum(tol, err_opt) + 1e-12)
-    assert info["fallback"] < nvel  # the network is used for some bins
-    assert np.all(length == 8) and index[-1] == 9 * nvel
+    print("trained in %.1f s (loss %.3g); table %.3f s, %d/%d bins from the network; "
+          "reference measure max: network %.2e optimiser %.2e table %.2e; relative max: "
+          "optimiser %.2e table %.2e (optimiser alone %.3f s)"
+          % (t_train, loss, info["seconds"], nvel - info["fallback"], nvel, en.max(), ref_opt.max(),
+             used.max(), rel_opt.max(), rel_tab.max(), t_opt))
+    # the table never keeps the worse of the two sets (FP64 judge; the table
+    # holds float copies, hence the small slack)
+    assert np.all(used <= np.minimum(en, np.maximum(ref_opt, tol)) * (1 + 1e-6) + 1e-12)
+    assert nvel - info["fallback"] > nvel // 2      # the network carries most bins
+    assert used.max() <= tol                          # every bin within the tolerance
+    assert rel_tab.max() < 0.2 * rel_opt.max()        # the gain at this operator length
+    assert np.all(length == M) and index[-1] == (M + 1) * nvel
