@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -109,6 +110,8 @@ struct rtm_ctx {
     int kv[2] = {RTM_KERNEL_X2_SPLIT, RTM_KERNEL_TILED};
     int nbl = 0;                           // shots per launch (<= B)
     int kstop = 0;                         // autotuning: time steps per phase (0: all)
+    bool pad_cells = false;                // pad update by k_pad (one thread per two cells)
+                                           // instead of k_pad_cols (RTM_PAD_CELLS=1)
     bool windowed = false;             // current batch uses per-shot models
     float *vs = nullptr, *r1s = nullptr;          // [B][NZ][P] window models
     int4 *meta_s = nullptr;
@@ -298,7 +301,7 @@ eng::StepArgs base_step(rtm_ctx *c)
 eng::PadArgs base_pad(rtm_ctx *c)
 {
     eng::PadArgs a{};
-    a.NZ = c->NZ; a.P = c->P; a.N2 = c->N2; a.M = c->M;
+    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2; a.M = c->M;
     a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
     a.nxs = c->gnx; a.rx0s = c->grx0;
     a.meta = c->windowed ? c->meta_s : c->pad_meta;
@@ -365,6 +368,21 @@ void join(rtm_ctx *c, int nh)
     cudaStreamWaitEvent(c->st, c->evf[1], 0);
 }
 
+// Pad update of a launch of n shots: the column-streaming kernel, or the
+// per-cell kernel when the context asks for it; `extra` threads record
+// receivers and quantise the previous step's 16-bit ring.
+void launch_pad(rtm_ctx *c, const eng::PadArgs &pa, int n, long extra, cudaStream_t st)
+{
+    if (c->pad_cells) {
+        const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT) + extra;
+        eng::k_pad<<<dim3(cdiv(npad, 256), n), 256, 0, st>>>(pa);
+        return;
+    }
+    const eng::PadTasks tk = eng::pad_tasks(c->NZ, c->NX, c->N2);
+    const unsigned bt = eng::PAD_WARPS * 32;
+    eng::k_pad_cols<<<dim3(tk.nblk + cdiv(extra, bt), n), bt, 0, st>>>(pa, tk);
+}
+
 // Forward run of nb shots (sources already in c->src).  rec_on: record the
 // receivers into c->rec (time-major [shot][NT][nrec]).
 int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
@@ -398,8 +416,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     RTM_LAUNCH_CHECK();
     eng::StepArgs sa = base_step(c);
     eng::PadArgs pa = base_pad(c);
-    const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT) + (rec_on ? c->nrec : 0) +
-                      (r16 ? c->ringsz : 0);
+    const long extra = (rec_on ? c->nrec : 0) + (r16 ? c->ringsz : 0);
     const int kend = c->kstop ? std::min(c->kstop, NT) : NT;  // kstop-2 steps when tuning
     Half hv[2];
     const int nh = halves(c, eng::MODE_FWD, nb, hv);
@@ -426,7 +443,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
             if (int rc = launch_step(c, eng::MODE_FWD, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 0);
             tic(c);
-            eng::k_pad<<<dim3(cdiv(npad, 256), hv[h].n), 256, 0, hv[h].st>>>(pa);
+            launch_pad(c, pa, hv[h].n, extra, hv[h].st);
             toc(c, 2);
         }
     }
@@ -456,7 +473,6 @@ int enqueue_backward(rtm_ctx *c, int nb)
     sa.nrec = c->nrec;
     sa.dstride = (long long)NT * c->nrec;
     eng::PadArgs pa = base_pad(c);
-    const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT);
     const int kend = c->kstop ? std::max(NT - c->kstop, 0) : 0;  // kstop-2 steps when tuning
     Half hv[2];
     const int nh = halves(c, eng::MODE_BWD, nb, hv);
@@ -479,7 +495,7 @@ int enqueue_backward(rtm_ctx *c, int nb)
             if (int rc = launch_step(c, eng::MODE_BWD, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 1);
             tic(c);
-            eng::k_pad<<<dim3(cdiv(npad, 256), hv[h].n), 256, 0, hv[h].st>>>(pa);
+            launch_pad(c, pa, hv[h].n, 0, hv[h].st);
             toc(c, 2);
         }
     }
@@ -708,6 +724,10 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     c->P = (c->NX + eng::TX - 1) / eng::TX * eng::TX;
     c->B = max_batch;
     c->nbl = max_batch;
+    {
+        const char *e = getenv("RTM_PAD_CELLS");
+        c->pad_cells = e && e[0] == '1';
+    }
     c->nrec = p->nrec;
     c->ss = (long long)c->NZ * c->P;
     c->ringsz = 2L * c->M * (c->nx + c->nz);

@@ -888,7 +888,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
 // ring save / restore, receiver recording.
 
 struct PadArgs {
-    int NZ, P, N2, M;
+    int NZ, NX, P, N2, M;     // NX: the widest grid of the launch
     int shot0;                // first shot of this launch (blockIdx.y + shot0)
     long long ss;
     long nabc;                // pad cells of the widest grid (threads per shot)
@@ -1002,6 +1002,26 @@ struct PadOut {
     long c, ri;
 };
 
+// One-way value and blend of a side cell (c, its inward neighbour n, lateral
+// offsets +-s): b = inv*(A*(u2n-u0n+u0c) - (-2u1c+u0c+u2n-2u1n+u0n) + Q*lat),
+// out = (1-w)*u2c + w*b, with f = {A, inv, Q, w}.
+__device__ __forceinline__ float pad_blend_side(float4 f, float pc, float u2n, float pnp, float pnm,
+                                                float u0c, float u0n, float u0p, float u0m, float u1c,
+                                                float u1n)
+{
+    const float lat = pnp - 2.0f * u2n + pnm + u0p - 2.0f * u0c + u0m;
+    const float bs = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1c + u0c + u2n - 2.0f * u1n + u0n) +
+                            f.z * lat);
+    return (1.0f - f.w) * pc + f.w * bs;
+}
+
+// Corner cell: b = inv*(u1c + r_1*(u2[c+dx] + u2[c+dz])), f = {r_1, inv, 0, w}.
+__device__ __forceinline__ float pad_blend_corner(float4 f, float pc, float u1c, float u2x, float u2z)
+{
+    const float bc = f.y * (u1c + f.x * (u2x + u2z));
+    return (1.0f - f.w) * pc + f.w * bc;
+}
+
 __device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long so, long t)
 {
     const int4 m = __ldg(a.meta + shot * a.tab_ss + t);
@@ -1012,12 +1032,9 @@ __device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long
     const float u2n = pr[n], pnp = pr[n + sd], pnm = pr[n - sd], pcz = pr[c + zc], pc = pr[c];
     const float u0c = u0[c], u0n = u0[n], u0p = u0[c + sd], u0m = u0[c - sd];
     const float u1c = u1[c], u1n = u1[n];
-    const float lat = pnp - 2.0f * u2n + pnm + u0p - 2.0f * u0c + u0m;
-    const float bs = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1c + u0c + u2n - 2.0f * u1n + u0n) +
-                            f.z * lat);
-    const float bc = f.y * (u1c + f.x * (u2n + pcz));
     PadOut r;
-    r.out = (1.0f - f.w) * pc + f.w * (corner ? bc : bs);
+    r.out = corner ? pad_blend_corner(f, pc, u1c, u2n, pcz)
+                   : pad_blend_side(f, pc, u2n, pnp, pnm, u0c, u0n, u0p, u0m, u1c, u1n);
     r.c = c;
     r.ri = a.ring_mode ? (long)(m.w >> 1) - 1 : -1;
     return r;
@@ -1087,6 +1104,173 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         bits = __reduce_max_sync(mask, bits);
         if ((threadIdx.x & 31) == __ffs(mask) - 1 && bits)
             atomicMax(a.amax + (long long)shot * a.slots + a.slot, bits);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Column-streaming form of the pad update (the same cells, formulas and
+// outputs as k_pad).  Each warp owns 30 adjacent columns of one band of the
+// pad (top, bottom, left or right) over a chunk of PAD_RCH rows, plus one halo
+// column on each side (lanes 0 and 31); every lane walks its column down the
+// rows with a three-row window of pre-blend values, u_{k-2} and u_{k-1}
+// loaded once per row (coalesced across the warp), and takes its x
+// neighbours from the adjacent lanes by shuffles.  The cell geometry follows
+// from (z, x) (abc_cell's classification), the model factors come from the
+// pad table at the cell's compact index.  Blocks beyond the bands' tasks do
+// the receiver recording and the 16-bit ring quantisation of k_pad's extra
+// threads.
+constexpr int PAD_RCH = 8;                 // rows per warp task
+constexpr int PAD_COLS = 30;               // columns a warp owns
+constexpr int PAD_WARPS = 4;               // warps per block
+
+struct PadTasks {
+    int ncg_tb, nch_tb;   // top / bottom bands: column groups, row chunks
+    int ncg_lr, nch_lr;   // left / right bands
+    int nblk;             // blocks of band tasks (the rest do recording / quantisation)
+};
+
+__host__ __device__ __forceinline__ PadTasks pad_tasks(int NZ, int NXmax, int N2)
+{
+    PadTasks t;
+    t.ncg_tb = (NXmax + PAD_COLS - 1) / PAD_COLS;
+    t.nch_tb = (N2 + PAD_RCH - 1) / PAD_RCH;
+    t.ncg_lr = (N2 + PAD_COLS - 1) / PAD_COLS;
+    t.nch_lr = (NZ - 2 * N2 + PAD_RCH - 1) / PAD_RCH;
+    const int ntask = 2 * t.ncg_tb * t.nch_tb + 2 * t.ncg_lr * t.nch_lr;
+    t.nblk = (ntask + PAD_WARPS - 1) / PAD_WARPS;
+    return t;
+}
+
+// Compact pad index of cell (z, x) in abc_cell's enumeration.
+__device__ __forceinline__ long pad_index(int z, int x, int NZ, int NX, int N2)
+{
+    if (z < N2) return (long)z * NX + x;
+    if (z >= NZ - N2) return (long)N2 * NX + (long)(z - (NZ - N2)) * NX + x;
+    return 2L * N2 * NX + (long)(z - N2) * (2 * N2) + (x < N2 ? x : x - (NX - 2 * N2));
+}
+
+__global__ void __launch_bounds__(PAD_WARPS * 32) k_pad_cols(const PadArgs a, const PadTasks tk)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int shot = blockIdx.y + a.shot0;
+    const long long so = (long long)shot * a.ss;
+    if ((int)blockIdx.x >= tk.nblk) {
+        // receiver recording and 16-bit quantisation (k_pad's extra threads)
+        long j = (long)(blockIdx.x - tk.nblk) * blockDim.x + threadIdx.x;
+        if (a.rec && j < a.nrec) {
+            const int z = a.rz0 + (int)j * a.rdz, x = a.rx0s[shot] + (int)j * a.rdx;
+            a.rec[(long long)shot * a.rec_ss + j] = a.a1[so + (long)z * a.P + x];
+            return;
+        }
+        if (a.rec) j -= a.nrec;
+        if (a.ring_prec && a.ring_mode == 1 && a.qslot >= 0 && j < a.ringsz) {
+            const long long sl = (long long)shot * a.slots + a.qslot;
+            const float mx = __uint_as_float(a.amax[sl]);
+            const float inv = mx > 0.0f ? RING16_TARGET / mx : 0.0f;
+            a.ring16[sl * a.ringsz + j] = ring_quant(a.qstage[(long long)shot * a.ringsz + j], inv, a.ring_prec);
+            if (j == 0) a.scale[sl] = mx / RING16_TARGET;
+        }
+        return;
+    }
+    const int NZ = a.NZ, N2 = a.N2, P = a.P;
+    const int NX = a.tab_ss ? a.nxs[shot] : a.NX;
+    // the warp's task: band, column group, row chunk
+    int task = blockIdx.x * PAD_WARPS + warp;
+    const int ntb = tk.ncg_tb * tk.nch_tb, nlr = tk.ncg_lr * tk.nch_lr;
+    int r0, r1, c0, c1, cg, ch;
+    if (task < 2 * ntb) {
+        const int band = task / ntb;
+        task -= band * ntb;
+        cg = task / tk.nch_tb;
+        ch = task - cg * tk.nch_tb;
+        r0 = band ? NZ - N2 : 0;
+        r1 = r0 + N2;
+        c0 = 0;
+        c1 = NX;
+    } else {
+        task -= 2 * ntb;
+        if (task >= 2 * nlr) return;
+        const int band = task / nlr;
+        task -= band * nlr;
+        cg = task / tk.nch_lr;
+        ch = task - cg * tk.nch_lr;
+        r0 = N2;
+        r1 = NZ - N2;
+        c0 = band ? NX - N2 : 0;
+        c1 = c0 + N2;
+    }
+    const int xg = c0 + cg * PAD_COLS;
+    if (xg >= c1) return;  // column group beyond this shot's (narrower) grid
+    const int zb = r0 + ch * PAD_RCH, ze = min(zb + PAD_RCH, r1);
+    const int x = xg + lane - 1;
+    const bool own = lane >= 1 && lane <= PAD_COLS && x < c1;
+    const int xc = min(max(x, 0), NX - 1);  // clamped column for the loads
+    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so;
+    const float4 *fac = a.fac + shot * a.tab_ss;
+    const int ex = min(x, NX - 1 - x), dx = (x < NX - 1 - x) ? 1 : -1;
+    const int nz = NZ - 2 * N2, nxi = NX - 2 * N2;
+    // window of rows z-1, z, z+1 of the lane's column
+    float p_m, p_c, p_p, v0_m, v0_c, v0_p, v1_m, v1_c, v1_p;
+    {
+        const int zm = max(zb - 1, 0), zc = zb, zp = min(zb + 1, NZ - 1);
+        p_m = pr[(long)zm * P + xc]; p_c = pr[(long)zc * P + xc]; p_p = pr[(long)zp * P + xc];
+        v0_m = u0[(long)zm * P + xc]; v0_c = u0[(long)zc * P + xc]; v0_p = u0[(long)zp * P + xc];
+        v1_m = u1[(long)zm * P + xc]; v1_c = u1[(long)zc * P + xc]; v1_p = u1[(long)zp * P + xc];
+    }
+    unsigned bits = 0u;
+#pragma unroll
+    for (int i = 0; i < PAD_RCH; ++i) {
+        const int z = zb + i;
+        if (z >= ze) break;  // warp-uniform
+        // next row of the window, loaded before this row's arithmetic
+        const int zn = min(z + 2, NZ - 1);
+        const float p_n = pr[(long)zn * P + xc], v0_n = u0[(long)zn * P + xc], v1_n = u1[(long)zn * P + xc];
+        // x neighbours from the adjacent lanes (every lane takes part)
+        const float pmL = __shfl_up_sync(0xffffffffu, p_m, 1), pmR = __shfl_down_sync(0xffffffffu, p_m, 1);
+        const float pcL = __shfl_up_sync(0xffffffffu, p_c, 1), pcR = __shfl_down_sync(0xffffffffu, p_c, 1);
+        const float ppL = __shfl_up_sync(0xffffffffu, p_p, 1), ppR = __shfl_down_sync(0xffffffffu, p_p, 1);
+        const float v0L = __shfl_up_sync(0xffffffffu, v0_c, 1), v0R = __shfl_down_sync(0xffffffffu, v0_c, 1);
+        const float v1L = __shfl_up_sync(0xffffffffu, v1_c, 1), v1R = __shfl_down_sync(0xffffffffu, v1_c, 1);
+        if (own) {
+            const int ez = min(z, NZ - 1 - z), dz = (z < NZ - 1 - z) ? 1 : -1;
+            const float4 f = __ldg(fac + pad_index(z, x, NZ, NX, N2));
+            float out;
+            if (ex >= ez + 2) {         // row edge: inward dz rows, lateral +-1 column
+                const float u2n = dz > 0 ? p_p : p_m, pnp = dz > 0 ? ppR : pmR, pnm = dz > 0 ? ppL : pmL;
+                const float u0n = dz > 0 ? v0_p : v0_m, u1n = dz > 0 ? v1_p : v1_m;
+                out = pad_blend_side(f, p_c, u2n, pnp, pnm, v0_c, u0n, v0R, v0L, v1_c, u1n);
+            } else if (ez >= ex + 2) {  // column edge: inward dx columns, lateral +-1 row
+                const float u2n = dx > 0 ? pcR : pcL, pnp = dx > 0 ? ppR : ppL, pnm = dx > 0 ? pmR : pmL;
+                const float u0n = dx > 0 ? v0R : v0L, u1n = dx > 0 ? v1R : v1L;
+                out = pad_blend_side(f, p_c, u2n, pnp, pnm, v0_c, u0n, v0_p, v0_m, v1_c, u1n);
+            } else {                    // corner
+                out = pad_blend_corner(f, p_c, v1_c, dx > 0 ? pcR : pcL, dz > 0 ? p_p : p_m);
+            }
+            const long cidx = (long)z * P + x;
+            a.a2[so + cidx] = out;
+            const long ri = (a.ring_mode && a.M > 0) ? ring_index(z, x, NZ, NX, N2, a.M, nz, nxi) : -1;
+            if (ri >= 0) {
+                if (a.ring_prec == 0) {
+                    if (a.ring_mode == 1)
+                        a.ring[(long long)shot * a.ring_ss + ri] = out;
+                    else
+                        a.s2[so + cidx] = a.ring[(long long)shot * a.ring_ss + ri];
+                } else if (a.ring_mode == 1) {
+                    a.stage[(long long)shot * a.ringsz + ri] = out;
+                    bits = max(bits, __float_as_uint(fabsf(out)));
+                } else {
+                    const long long sl = (long long)shot * a.slots + a.slot;
+                    a.s2[so + cidx] = ring_dequant(a.ring16[sl * a.ringsz + ri], a.scale[sl], a.ring_prec);
+                }
+            }
+        }
+        p_m = p_c; p_c = p_p; p_p = p_n;
+        v0_m = v0_c; v0_c = v0_p; v0_p = v0_n;
+        v1_m = v1_c; v1_c = v1_p; v1_p = v1_n;
+    }
+    if (a.ring_prec && a.ring_mode == 1) {
+        bits = __reduce_max_sync(0xffffffffu, bits);
+        if (lane == 0 && bits) atomicMax(a.amax + (long long)shot * a.slots + a.slot, bits);
     }
 }
 
