@@ -1032,9 +1032,14 @@ __device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long
     const float u2n = pr[n], pnp = pr[n + sd], pnm = pr[n - sd], pcz = pr[c + zc], pc = pr[c];
     const float u0c = u0[c], u0n = u0[n], u0p = u0[c + sd], u0m = u0[c - sd];
     const float u1c = u1[c], u1n = u1[n];
+    // both formulas, then a select: no branch on the cell's kind, so the
+    // loads of a thread's cells stay in flight together
+    const float lat = pnp - 2.0f * u2n + pnm + u0p - 2.0f * u0c + u0m;
+    const float bs = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1c + u0c + u2n - 2.0f * u1n + u0n) +
+                            f.z * lat);
+    const float bc = f.y * (u1c + f.x * (u2n + pcz));
     PadOut r;
-    r.out = corner ? pad_blend_corner(f, pc, u1c, u2n, pcz)
-                   : pad_blend_side(f, pc, u2n, pnp, pnm, u0c, u0n, u0p, u0m, u1c, u1n);
+    r.out = (1.0f - f.w) * pc + f.w * (corner ? bc : bs);
     r.c = c;
     r.ri = a.ring_mode ? (long)(m.w >> 1) - 1 : -1;
     return r;
@@ -1119,7 +1124,10 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
 // pad table at the cell's compact index.  Blocks beyond the bands' tasks do
 // the receiver recording and the 16-bit ring quantisation of k_pad's extra
 // threads.
-constexpr int PAD_RCH = 8;                 // rows per warp task
+#ifndef RTM_PAD_RCH
+#define RTM_PAD_RCH 8
+#endif
+constexpr int PAD_RCH = RTM_PAD_RCH;       // rows per warp task
 constexpr int PAD_COLS = 30;               // columns a warp owns
 constexpr int PAD_WARPS = 4;               // warps per block
 
@@ -1205,26 +1213,38 @@ __global__ void __launch_bounds__(PAD_WARPS * 32) k_pad_cols(const PadArgs a, co
     const int x = xg + lane - 1;
     const bool own = lane >= 1 && lane <= PAD_COLS && x < c1;
     const int xc = min(max(x, 0), NX - 1);  // clamped column for the loads
-    const float *u0 = a.a0 + so, *u1 = a.a1 + so, *pr = a.pre + so;
-    const float4 *fac = a.fac + shot * a.tab_ss;
+    const float *__restrict__ u0 = a.a0 + so;
+    const float *__restrict__ u1 = a.a1 + so;
+    const float *__restrict__ pr = a.pre + so;
+    const float4 *__restrict__ fac = a.fac + shot * a.tab_ss;
     const int ex = min(x, NX - 1 - x), dx = (x < NX - 1 - x) ? 1 : -1;
     const int nz = NZ - 2 * N2, nxi = NX - 2 * N2;
-    // window of rows z-1, z, z+1 of the lane's column
-    float p_m, p_c, p_p, v0_m, v0_c, v0_p, v1_m, v1_c, v1_p;
-    {
-        const int zm = max(zb - 1, 0), zc = zb, zp = min(zb + 1, NZ - 1);
-        p_m = pr[(long)zm * P + xc]; p_c = pr[(long)zc * P + xc]; p_p = pr[(long)zp * P + xc];
-        v0_m = u0[(long)zm * P + xc]; v0_c = u0[(long)zc * P + xc]; v0_p = u0[(long)zp * P + xc];
-        v1_m = u1[(long)zm * P + xc]; v1_c = u1[(long)zc * P + xc]; v1_p = u1[(long)zp * P + xc];
+    // every row the task reads (zb-1 .. zb+PAD_RCH) and the model factors of
+    // its cells, loaded before any arithmetic so that all loads are in flight
+    // together (rows and factors beyond the grid or the chunk are clamped
+    // and unused)
+    float pw[PAD_RCH + 2], w0[PAD_RCH + 2], w1[PAD_RCH + 2];
+    float4 fw[PAD_RCH];
+#pragma unroll
+    for (int j = 0; j < PAD_RCH + 2; ++j) {
+        const long o = (long)min(max(zb - 1 + j, 0), NZ - 1) * P + xc;
+        pw[j] = pr[o];
+        w0[j] = u0[o];
+        w1[j] = u1[o];
+    }
+#pragma unroll
+    for (int i = 0; i < PAD_RCH; ++i) {
+        const int z = min(zb + i, ze - 1);
+        fw[i] = own ? __ldg(fac + pad_index(z, x, NZ, NX, N2)) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     unsigned bits = 0u;
 #pragma unroll
     for (int i = 0; i < PAD_RCH; ++i) {
         const int z = zb + i;
         if (z >= ze) break;  // warp-uniform
-        // next row of the window, loaded before this row's arithmetic
-        const int zn = min(z + 2, NZ - 1);
-        const float p_n = pr[(long)zn * P + xc], v0_n = u0[(long)zn * P + xc], v1_n = u1[(long)zn * P + xc];
+        const float p_m = pw[i], p_c = pw[i + 1], p_p = pw[i + 2];
+        const float v0_m = w0[i], v0_c = w0[i + 1], v0_p = w0[i + 2];
+        const float v1_m = w1[i], v1_c = w1[i + 1], v1_p = w1[i + 2];
         // x neighbours from the adjacent lanes (every lane takes part)
         const float pmL = __shfl_up_sync(0xffffffffu, p_m, 1), pmR = __shfl_down_sync(0xffffffffu, p_m, 1);
         const float pcL = __shfl_up_sync(0xffffffffu, p_c, 1), pcR = __shfl_down_sync(0xffffffffu, p_c, 1);
@@ -1233,7 +1253,7 @@ __global__ void __launch_bounds__(PAD_WARPS * 32) k_pad_cols(const PadArgs a, co
         const float v1L = __shfl_up_sync(0xffffffffu, v1_c, 1), v1R = __shfl_down_sync(0xffffffffu, v1_c, 1);
         if (own) {
             const int ez = min(z, NZ - 1 - z), dz = (z < NZ - 1 - z) ? 1 : -1;
-            const float4 f = __ldg(fac + pad_index(z, x, NZ, NX, N2));
+            const float4 f = fw[i];
             float out;
             if (ex >= ez + 2) {         // row edge: inward dz rows, lateral +-1 column
                 const float u2n = dz > 0 ? p_p : p_m, pnp = dz > 0 ? ppR : pmR, pnm = dz > 0 ? ppL : pmL;
@@ -1264,9 +1284,6 @@ __global__ void __launch_bounds__(PAD_WARPS * 32) k_pad_cols(const PadArgs a, co
                 }
             }
         }
-        p_m = p_c; p_c = p_p; p_p = p_n;
-        v0_m = v0_c; v0_c = v0_p; v0_p = v0_n;
-        v1_m = v1_c; v1_c = v1_p; v1_p = v1_n;
     }
     if (a.ring_prec && a.ring_mode == 1) {
         bits = __reduce_max_sync(0xffffffffu, bits);

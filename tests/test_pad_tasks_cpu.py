@@ -7,18 +7,19 @@ wider launch, and small odd shapes."""
 import numpy as np
 import pytest
 
-RCH, COLS, WARPS = 8, 30, 4  # PAD_RCH, PAD_COLS, PAD_WARPS
+COLS, WARPS = 30, 4  # PAD_COLS, PAD_WARPS (PAD_RCH, the rows per task, is a build
+                     # parameter: 8 by default, checked at 4, 8 and 16)
 
 
-def tasks(NZ, NXmax, N2):
+def tasks(NZ, NXmax, N2, RCH):
     ncg_tb, nch_tb = -(-NXmax // COLS), -(-N2 // RCH)
     ncg_lr, nch_lr = -(-N2 // COLS), -(-(NZ - 2 * N2) // RCH)
     ntask = 2 * ncg_tb * nch_tb + 2 * ncg_lr * nch_lr
     return ncg_tb, nch_tb, ncg_lr, nch_lr, -(-ntask // WARPS)
 
 
-def owned_cells(NZ, NX, NXmax, N2):
-    ncg_tb, nch_tb, ncg_lr, nch_lr, nblk = tasks(NZ, NXmax, N2)
+def owned_cells(NZ, NX, NXmax, N2, RCH):
+    ncg_tb, nch_tb, ncg_lr, nch_lr, nblk = tasks(NZ, NXmax, N2, RCH)
     ntb, nlr = ncg_tb * nch_tb, ncg_lr * nch_lr
     count = np.zeros((NZ, NX), np.int32)
     for task in range(nblk * WARPS):
@@ -45,9 +46,9 @@ def owned_cells(NZ, NX, NXmax, N2):
             x = xg + lane - 1
             xc = min(max(x, 0), NX - 1)
             assert 0 <= xc < NX
+            for j in range(RCH + 2):  # the rows a task loads, clamped
+                assert 0 <= min(max(zb - 1 + j, 0), NZ - 1) < NZ
             for z in range(zb, ze):
-                for zr in (max(z - 1, 0), z, min(z + 1, NZ - 1), min(z + 2, NZ - 1)):
-                    assert 0 <= zr < NZ
                 if 1 <= lane <= COLS and x < c1:
                     assert 0 <= z < NZ and 0 <= x < NX
                     count[z, x] += 1
@@ -62,8 +63,9 @@ def owned_cells(NZ, NX, NXmax, N2):
     (37, 53, 61, 5),
     (140, 140, 140, 64),      # pad wider than a column group
 ])
-def test_every_pad_cell_owned_once(NZ, NX, NXmax, N2):
-    count = owned_cells(NZ, NX, NXmax, N2)
+@pytest.mark.parametrize("RCH", [4, 8, 16])
+def test_every_pad_cell_owned_once(NZ, NX, NXmax, N2, RCH):
+    count = owned_cells(NZ, NX, NXmax, N2, RCH)
     pad = np.ones((NZ, NX), bool)
     pad[N2:NZ - N2, N2:NX - N2] = False
     assert np.all(count[pad] == 1)
