@@ -83,7 +83,7 @@ def parse():
     ap.add_argument("--nt", type=int, default=0, help="time steps (0: the workload's own count)")
     ap.add_argument("--batch", type=int, default=0, help="shots per batch (0: all)")
     ap.add_argument("--coef", default="adaptive", choices=["adaptive", "taylor"])
-    ap.add_argument("--ring", default=None, choices=["f32", "bf16", "f16"],
+    ap.add_argument("--ring", default=None, choices=["f32", "bf16", "f16", "i16"],
                     help="boundary-ring storage (stencil and imaging stay FP32); default f16 "
                          "for the multi-shot workload, f32 for rvsp (FP32 throughout), bf16 for c5")
     ap.add_argument("--no-plain", action="store_true",
@@ -516,7 +516,7 @@ def run_rvsp(a, cfg):
     del tmp
     # sources in each shot's own padded grid
     wsrc = [z * (int(w) + 2 * cfg.N2) + (x - int(x0)) for (z, x), x0, w in zip(src, xa, wn)]
-    ring = {"f32": capi.RTM_RING_F32, "bf16": capi.RTM_RING_BF16, "f16": capi.RTM_RING_F16}[cfg.ring]
+    ring = ring_flag(cfg)
     eng = Engine(pmig, batch=batch, stream=sh, ring_precision=ring)
     tuned = None
     if a.kernel == "auto":
@@ -743,7 +743,8 @@ def step_gathers(Engine, ptrue, pmig, src, batch, stream_handle, torch):
 
 def ring_flag(cfg):
     from rtm_gpu_gb300 import capi
-    return {"f32": capi.RTM_RING_F32, "bf16": capi.RTM_RING_BF16, "f16": capi.RTM_RING_F16}[cfg.ring]
+    return {"f32": capi.RTM_RING_F32, "bf16": capi.RTM_RING_BF16, "f16": capi.RTM_RING_F16,
+            "i16": capi.RTM_RING_I16}[cfg.ring]
 
 
 def run_multishot(a, cfg):

@@ -229,10 +229,15 @@ typedef struct rtm_problem {
     /* receivers: cells (rz0 + j*rdz, rx0 + j*rdx), j < nrec (a surface line,
        a vertical well, ...); both steps 0 is invalid */
     int rz0, rx0, rdz, rdx, nrec;
-    int ring_precision; /* RTM_RING_F32 / RTM_RING_BF16 / RTM_RING_F16          */
+    int ring_precision; /* RTM_RING_F32 / _BF16 / _F16 / _I16                   */
 } rtm_problem;
 
-enum { RTM_RING_F32 = 0, RTM_RING_BF16 = 1, RTM_RING_F16 = 2 };
+/* Storage of the saved boundary rings (the stencil and imaging arithmetic
+ * stay FP32): FP32, or 16 bits with one FP32 scale per shot and step -- BF16
+ * or FP16 values scaled so the step's max |value| is 16384, or int16
+ * fractions of the step's max |value| (RTM_RING_I16: fixed point, the
+ * finest absolute rounding at the values that dominate the field). */
+enum { RTM_RING_F32 = 0, RTM_RING_BF16 = 1, RTM_RING_F16 = 2, RTM_RING_I16 = 3 };
 
 /* flags for rtm_model_batch / rtm_migrate_batch */
 enum {

@@ -18,7 +18,7 @@ _lib = None
 RTM_OK = 0
 RTM_DEVICE_PTRS = 1
 RTM_NO_GRAPH = 2
-RTM_RING_F32, RTM_RING_BF16, RTM_RING_F16 = 0, 1, 2
+RTM_RING_F32, RTM_RING_BF16, RTM_RING_F16, RTM_RING_I16 = 0, 1, 2, 3
 RTM_KERNEL_TILED, RTM_KERNEL_PERSISTENT, RTM_KERNEL_SPLIT, RTM_KERNEL_X2, RTM_KERNEL_X2_SPLIT = 0, 1, 2, 3, 4
 
 vp = C.c_void_p

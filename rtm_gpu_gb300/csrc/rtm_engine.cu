@@ -13,7 +13,6 @@
 
 #include <algorithm>
 #include <cstdio>
-#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -110,8 +109,6 @@ struct rtm_ctx {
     int kv[2] = {RTM_KERNEL_X2_SPLIT, RTM_KERNEL_TILED};
     int nbl = 0;                           // shots per launch (<= B)
     int kstop = 0;                         // autotuning: time steps per phase (0: all)
-    bool pad_cells = false;                // pad update by k_pad (one thread per two cells)
-                                           // instead of k_pad_cols (RTM_PAD_CELLS=1)
     bool windowed = false;             // current batch uses per-shot models
     float *vs = nullptr, *r1s = nullptr;          // [B][NZ][P] window models
     int4 *meta_s = nullptr;
@@ -301,7 +298,7 @@ eng::StepArgs base_step(rtm_ctx *c)
 eng::PadArgs base_pad(rtm_ctx *c)
 {
     eng::PadArgs a{};
-    a.NZ = c->NZ; a.NX = c->NX; a.P = c->P; a.N2 = c->N2; a.M = c->M;
+    a.NZ = c->NZ; a.P = c->P; a.N2 = c->N2; a.M = c->M;
     a.ss = c->ss; a.nabc = abc_count(c->NZ, c->NX, c->N2);
     a.nxs = c->gnx; a.rx0s = c->grx0;
     a.meta = c->windowed ? c->meta_s : c->pad_meta;
@@ -368,19 +365,12 @@ void join(rtm_ctx *c, int nh)
     cudaStreamWaitEvent(c->st, c->evf[1], 0);
 }
 
-// Pad update of a launch of n shots: the column-streaming kernel, or the
-// per-cell kernel when the context asks for it; `extra` threads record
-// receivers and quantise the previous step's 16-bit ring.
+// Pad update of a launch of n shots; `extra` threads record receivers and
+// quantise the previous step's 16-bit ring.
 void launch_pad(rtm_ctx *c, const eng::PadArgs &pa, int n, long extra, cudaStream_t st)
 {
-    if (c->pad_cells) {
-        const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT) + extra;
-        eng::k_pad<<<dim3(cdiv(npad, 256), n), 256, 0, st>>>(pa);
-        return;
-    }
-    const eng::PadTasks tk = eng::pad_tasks(c->NZ, c->NX, c->N2);
-    const unsigned bt = eng::PAD_WARPS * 32;
-    eng::k_pad_cols<<<dim3(tk.nblk + cdiv(extra, bt), n), bt, 0, st>>>(pa, tk);
+    const long npad = cdiv(abc_count(c->NZ, c->NX, c->N2), eng::PAD_CPT) + extra;
+    eng::k_pad<<<dim3(cdiv(npad, 256), n), 256, 0, st>>>(pa);
 }
 
 // Forward run of nb shots (sources already in c->src).  rec_on: record the
@@ -709,7 +699,7 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     *out = nullptr;
     if (p->nz < 1 || p->nx < 1 || p->N2 < 2 || p->M < 0 || p->M > p->N2 || p->NT < 4 || !p->v ||
         !p->r1 || !p->w || !p->coef || !p->wav || (p->adaptive && (!p->index || p->nbins < 1)) ||
-        p->ring_precision < RTM_RING_F32 || p->ring_precision > RTM_RING_F16) {
+        p->ring_precision < RTM_RING_F32 || p->ring_precision > RTM_RING_I16) {
         rtm_set_last_error("rtm_ctx_create: invalid problem");
         return RTM_ERR_ARG;
     }
@@ -724,10 +714,6 @@ int rtm_ctx_create(rtm_ctx **out, const rtm_problem *p, int max_batch, rtm_strea
     c->P = (c->NX + eng::TX - 1) / eng::TX * eng::TX;
     c->B = max_batch;
     c->nbl = max_batch;
-    {
-        const char *e = getenv("RTM_PAD_CELLS");
-        c->pad_cells = e && e[0] == '1';
-    }
     c->nrec = p->nrec;
     c->ss = (long long)c->NZ * c->P;
     c->ringsz = 2L * c->M * (c->nx + c->nz);

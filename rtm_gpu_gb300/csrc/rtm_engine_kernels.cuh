@@ -888,7 +888,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
 // ring save / restore, receiver recording.
 
 struct PadArgs {
-    int NZ, NX, P, N2, M;     // NX: the widest grid of the launch
+    int NZ, P, N2, M;
     int shot0;                // first shot of this launch (blockIdx.y + shot0)
     long long ss;
     long nabc;                // pad cells of the widest grid (threads per shot)
@@ -909,7 +909,7 @@ struct PadArgs {
     float *rec;
     long long rec_ss;
     int rz0, rx0, rdz, rdx, nrec;
-    // 16-bit ring store (ring_prec 1: bf16, 2: fp16) with per-step max-abs
+    // 16-bit ring store (ring_prec 1: bf16, 2: fp16, 3: int16) with per-step max-abs
     // scaling.  Forward: the blended ring values of step k go to the FP32
     // stage (stage + shot*ringsz) and their max |value| to amax[shot][k];
     // the quantisation of slot qslot (= k-1, whose max is final by now) from
@@ -926,17 +926,31 @@ struct PadArgs {
     int slot, qslot;         // slot written (fwd) / restored (bwd); slot to quantise (<0: none)
 };
 
-constexpr float RING16_TARGET = 16384.0f;  // max |value| maps here (fp16 max is 65504)
+// Value a step's max |ring value| maps to: 16384 for FP16 / BF16 (FP16 keeps
+// headroom below 65504; BF16 uses the same scale), 32767 for the scaled
+// integers of RTM_RING_I16, whose values then fill the int16 range.
+__host__ __device__ __forceinline__ float ring16_target(int prec) { return prec == 3 ? 32767.0f : 16384.0f; }
 
+// 16-bit ring codes: 1 BF16, 2 FP16 (floating point: relative rounding
+// 2^-9 / 2^-12 of each value), 3 int16 (a fixed-point fraction of the step's
+// largest value: absolute rounding of half of max/32767 for every value,
+// 16 times finer than FP16 at the largest values that dominate the field).
 __device__ __forceinline__ uint16_t ring_quant(float v, float inv, int prec)
 {
     if (prec == 1) return __bfloat16_as_ushort(__float2bfloat16_rn(v * inv));
+    if (prec == 3) {
+        const int q = __float2int_rn(v * inv);  // |v| <= the step's max, so |q| <= 32767
+        return (uint16_t)(short)max(-32767, min(32767, q));
+    }
     return __half_as_ushort(__float2half_rn(v * inv));
 }
 
 __device__ __forceinline__ float ring_dequant(uint16_t q, float sc, int prec)
 {
-    const float f = prec == 1 ? __bfloat162float(__ushort_as_bfloat16(q)) : __half2float(__ushort_as_half(q));
+    float f;
+    if (prec == 1) f = __bfloat162float(__ushort_as_bfloat16(q));
+    else if (prec == 3) f = (float)(short)q;
+    else f = __half2float(__ushort_as_half(q));
     return f * sc;
 }
 
@@ -1002,26 +1016,6 @@ struct PadOut {
     long c, ri;
 };
 
-// One-way value and blend of a side cell (c, its inward neighbour n, lateral
-// offsets +-s): b = inv*(A*(u2n-u0n+u0c) - (-2u1c+u0c+u2n-2u1n+u0n) + Q*lat),
-// out = (1-w)*u2c + w*b, with f = {A, inv, Q, w}.
-__device__ __forceinline__ float pad_blend_side(float4 f, float pc, float u2n, float pnp, float pnm,
-                                                float u0c, float u0n, float u0p, float u0m, float u1c,
-                                                float u1n)
-{
-    const float lat = pnp - 2.0f * u2n + pnm + u0p - 2.0f * u0c + u0m;
-    const float bs = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1c + u0c + u2n - 2.0f * u1n + u0n) +
-                            f.z * lat);
-    return (1.0f - f.w) * pc + f.w * bs;
-}
-
-// Corner cell: b = inv*(u1c + r_1*(u2[c+dx] + u2[c+dz])), f = {r_1, inv, 0, w}.
-__device__ __forceinline__ float pad_blend_corner(float4 f, float pc, float u1c, float u2x, float u2z)
-{
-    const float bc = f.y * (u1c + f.x * (u2x + u2z));
-    return (1.0f - f.w) * pc + f.w * bc;
-}
-
 __device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long so, long t)
 {
     const int4 m = __ldg(a.meta + shot * a.tab_ss + t);
@@ -1032,8 +1026,6 @@ __device__ __forceinline__ PadOut pad_cell(const PadArgs &a, int shot, long long
     const float u2n = pr[n], pnp = pr[n + sd], pnm = pr[n - sd], pcz = pr[c + zc], pc = pr[c];
     const float u0c = u0[c], u0n = u0[n], u0p = u0[c + sd], u0m = u0[c - sd];
     const float u1c = u1[c], u1n = u1[n];
-    // both formulas, then a select: no branch on the cell's kind, so the
-    // loads of a thread's cells stay in flight together
     const float lat = pnp - 2.0f * u2n + pnm + u0p - 2.0f * u0c + u0m;
     const float bs = f.y * (f.x * (u2n - u0n + u0c) - (-2.0f * u1c + u0c + u2n - 2.0f * u1n + u0n) +
                             f.z * lat);
@@ -1062,9 +1054,10 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         if (a.ring_prec && a.ring_mode == 1 && a.qslot >= 0 && j < a.ringsz) {
             const long long sl = (long long)shot * a.slots + a.qslot;
             const float mx = __uint_as_float(a.amax[sl]);
-            const float inv = mx > 0.0f ? RING16_TARGET / mx : 0.0f;
+            const float tgt = ring16_target(a.ring_prec);
+            const float inv = mx > 0.0f ? tgt / mx : 0.0f;
             a.ring16[sl * a.ringsz + j] = ring_quant(a.qstage[(long long)shot * a.ringsz + j], inv, a.ring_prec);
-            if (j == 0) a.scale[sl] = mx / RING16_TARGET;
+            if (j == 0) a.scale[sl] = mx / tgt;
         }
         return;
     }
@@ -1109,185 +1102,6 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
         bits = __reduce_max_sync(mask, bits);
         if ((threadIdx.x & 31) == __ffs(mask) - 1 && bits)
             atomicMax(a.amax + (long long)shot * a.slots + a.slot, bits);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Column-streaming form of the pad update (the same cells, formulas and
-// outputs as k_pad).  Each warp owns 30 adjacent columns of one band of the
-// pad (top, bottom, left or right) over a chunk of PAD_RCH rows, plus one halo
-// column on each side (lanes 0 and 31); every lane walks its column down the
-// rows with a three-row window of pre-blend values, u_{k-2} and u_{k-1}
-// loaded once per row (coalesced across the warp), and takes its x
-// neighbours from the adjacent lanes by shuffles.  The cell geometry follows
-// from (z, x) (abc_cell's classification), the model factors come from the
-// pad table at the cell's compact index.  Blocks beyond the bands' tasks do
-// the receiver recording and the 16-bit ring quantisation of k_pad's extra
-// threads.
-#ifndef RTM_PAD_RCH
-#define RTM_PAD_RCH 8
-#endif
-constexpr int PAD_RCH = RTM_PAD_RCH;       // rows per warp task
-constexpr int PAD_COLS = 30;               // columns a warp owns
-constexpr int PAD_WARPS = 4;               // warps per block
-
-struct PadTasks {
-    int ncg_tb, nch_tb;   // top / bottom bands: column groups, row chunks
-    int ncg_lr, nch_lr;   // left / right bands
-    int nblk;             // blocks of band tasks (the rest do recording / quantisation)
-};
-
-__host__ __device__ __forceinline__ PadTasks pad_tasks(int NZ, int NXmax, int N2)
-{
-    PadTasks t;
-    t.ncg_tb = (NXmax + PAD_COLS - 1) / PAD_COLS;
-    t.nch_tb = (N2 + PAD_RCH - 1) / PAD_RCH;
-    t.ncg_lr = (N2 + PAD_COLS - 1) / PAD_COLS;
-    t.nch_lr = (NZ - 2 * N2 + PAD_RCH - 1) / PAD_RCH;
-    const int ntask = 2 * t.ncg_tb * t.nch_tb + 2 * t.ncg_lr * t.nch_lr;
-    t.nblk = (ntask + PAD_WARPS - 1) / PAD_WARPS;
-    return t;
-}
-
-// Compact pad index of cell (z, x) in abc_cell's enumeration.
-__device__ __forceinline__ long pad_index(int z, int x, int NZ, int NX, int N2)
-{
-    if (z < N2) return (long)z * NX + x;
-    if (z >= NZ - N2) return (long)N2 * NX + (long)(z - (NZ - N2)) * NX + x;
-    return 2L * N2 * NX + (long)(z - N2) * (2 * N2) + (x < N2 ? x : x - (NX - 2 * N2));
-}
-
-__global__ void __launch_bounds__(PAD_WARPS * 32) k_pad_cols(const PadArgs a, const PadTasks tk)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int shot = blockIdx.y + a.shot0;
-    const long long so = (long long)shot * a.ss;
-    if ((int)blockIdx.x >= tk.nblk) {
-        // receiver recording and 16-bit quantisation (k_pad's extra threads)
-        long j = (long)(blockIdx.x - tk.nblk) * blockDim.x + threadIdx.x;
-        if (a.rec && j < a.nrec) {
-            const int z = a.rz0 + (int)j * a.rdz, x = a.rx0s[shot] + (int)j * a.rdx;
-            a.rec[(long long)shot * a.rec_ss + j] = a.a1[so + (long)z * a.P + x];
-            return;
-        }
-        if (a.rec) j -= a.nrec;
-        if (a.ring_prec && a.ring_mode == 1 && a.qslot >= 0 && j < a.ringsz) {
-            const long long sl = (long long)shot * a.slots + a.qslot;
-            const float mx = __uint_as_float(a.amax[sl]);
-            const float inv = mx > 0.0f ? RING16_TARGET / mx : 0.0f;
-            a.ring16[sl * a.ringsz + j] = ring_quant(a.qstage[(long long)shot * a.ringsz + j], inv, a.ring_prec);
-            if (j == 0) a.scale[sl] = mx / RING16_TARGET;
-        }
-        return;
-    }
-    const int NZ = a.NZ, N2 = a.N2, P = a.P;
-    const int NX = a.tab_ss ? a.nxs[shot] : a.NX;
-    // the warp's task: band, column group, row chunk
-    int task = blockIdx.x * PAD_WARPS + warp;
-    const int ntb = tk.ncg_tb * tk.nch_tb, nlr = tk.ncg_lr * tk.nch_lr;
-    int r0, r1, c0, c1, cg, ch;
-    if (task < 2 * ntb) {
-        const int band = task / ntb;
-        task -= band * ntb;
-        cg = task / tk.nch_tb;
-        ch = task - cg * tk.nch_tb;
-        r0 = band ? NZ - N2 : 0;
-        r1 = r0 + N2;
-        c0 = 0;
-        c1 = NX;
-    } else {
-        task -= 2 * ntb;
-        if (task >= 2 * nlr) return;
-        const int band = task / nlr;
-        task -= band * nlr;
-        cg = task / tk.nch_lr;
-        ch = task - cg * tk.nch_lr;
-        r0 = N2;
-        r1 = NZ - N2;
-        c0 = band ? NX - N2 : 0;
-        c1 = c0 + N2;
-    }
-    const int xg = c0 + cg * PAD_COLS;
-    if (xg >= c1) return;  // column group beyond this shot's (narrower) grid
-    const int zb = r0 + ch * PAD_RCH, ze = min(zb + PAD_RCH, r1);
-    const int x = xg + lane - 1;
-    const bool own = lane >= 1 && lane <= PAD_COLS && x < c1;
-    const int xc = min(max(x, 0), NX - 1);  // clamped column for the loads
-    const float *__restrict__ u0 = a.a0 + so;
-    const float *__restrict__ u1 = a.a1 + so;
-    const float *__restrict__ pr = a.pre + so;
-    const float4 *__restrict__ fac = a.fac + shot * a.tab_ss;
-    const int ex = min(x, NX - 1 - x), dx = (x < NX - 1 - x) ? 1 : -1;
-    const int nz = NZ - 2 * N2, nxi = NX - 2 * N2;
-    // every row the task reads (zb-1 .. zb+PAD_RCH) and the model factors of
-    // its cells, loaded before any arithmetic so that all loads are in flight
-    // together (rows and factors beyond the grid or the chunk are clamped
-    // and unused)
-    float pw[PAD_RCH + 2], w0[PAD_RCH + 2], w1[PAD_RCH + 2];
-    float4 fw[PAD_RCH];
-#pragma unroll
-    for (int j = 0; j < PAD_RCH + 2; ++j) {
-        const long o = (long)min(max(zb - 1 + j, 0), NZ - 1) * P + xc;
-        pw[j] = pr[o];
-        w0[j] = u0[o];
-        w1[j] = u1[o];
-    }
-#pragma unroll
-    for (int i = 0; i < PAD_RCH; ++i) {
-        const int z = min(zb + i, ze - 1);
-        fw[i] = own ? __ldg(fac + pad_index(z, x, NZ, NX, N2)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    unsigned bits = 0u;
-#pragma unroll
-    for (int i = 0; i < PAD_RCH; ++i) {
-        const int z = zb + i;
-        if (z >= ze) break;  // warp-uniform
-        const float p_m = pw[i], p_c = pw[i + 1], p_p = pw[i + 2];
-        const float v0_m = w0[i], v0_c = w0[i + 1], v0_p = w0[i + 2];
-        const float v1_m = w1[i], v1_c = w1[i + 1], v1_p = w1[i + 2];
-        // x neighbours from the adjacent lanes (every lane takes part)
-        const float pmL = __shfl_up_sync(0xffffffffu, p_m, 1), pmR = __shfl_down_sync(0xffffffffu, p_m, 1);
-        const float pcL = __shfl_up_sync(0xffffffffu, p_c, 1), pcR = __shfl_down_sync(0xffffffffu, p_c, 1);
-        const float ppL = __shfl_up_sync(0xffffffffu, p_p, 1), ppR = __shfl_down_sync(0xffffffffu, p_p, 1);
-        const float v0L = __shfl_up_sync(0xffffffffu, v0_c, 1), v0R = __shfl_down_sync(0xffffffffu, v0_c, 1);
-        const float v1L = __shfl_up_sync(0xffffffffu, v1_c, 1), v1R = __shfl_down_sync(0xffffffffu, v1_c, 1);
-        if (own) {
-            const int ez = min(z, NZ - 1 - z), dz = (z < NZ - 1 - z) ? 1 : -1;
-            const float4 f = fw[i];
-            float out;
-            if (ex >= ez + 2) {         // row edge: inward dz rows, lateral +-1 column
-                const float u2n = dz > 0 ? p_p : p_m, pnp = dz > 0 ? ppR : pmR, pnm = dz > 0 ? ppL : pmL;
-                const float u0n = dz > 0 ? v0_p : v0_m, u1n = dz > 0 ? v1_p : v1_m;
-                out = pad_blend_side(f, p_c, u2n, pnp, pnm, v0_c, u0n, v0R, v0L, v1_c, u1n);
-            } else if (ez >= ex + 2) {  // column edge: inward dx columns, lateral +-1 row
-                const float u2n = dx > 0 ? pcR : pcL, pnp = dx > 0 ? ppR : ppL, pnm = dx > 0 ? pmR : pmL;
-                const float u0n = dx > 0 ? v0R : v0L, u1n = dx > 0 ? v1R : v1L;
-                out = pad_blend_side(f, p_c, u2n, pnp, pnm, v0_c, u0n, v0_p, v0_m, v1_c, u1n);
-            } else {                    // corner
-                out = pad_blend_corner(f, p_c, v1_c, dx > 0 ? pcR : pcL, dz > 0 ? p_p : p_m);
-            }
-            const long cidx = (long)z * P + x;
-            a.a2[so + cidx] = out;
-            const long ri = (a.ring_mode && a.M > 0) ? ring_index(z, x, NZ, NX, N2, a.M, nz, nxi) : -1;
-            if (ri >= 0) {
-                if (a.ring_prec == 0) {
-                    if (a.ring_mode == 1)
-                        a.ring[(long long)shot * a.ring_ss + ri] = out;
-                    else
-                        a.s2[so + cidx] = a.ring[(long long)shot * a.ring_ss + ri];
-                } else if (a.ring_mode == 1) {
-                    a.stage[(long long)shot * a.ringsz + ri] = out;
-                    bits = max(bits, __float_as_uint(fabsf(out)));
-                } else {
-                    const long long sl = (long long)shot * a.slots + a.slot;
-                    a.s2[so + cidx] = ring_dequant(a.ring16[sl * a.ringsz + ri], a.scale[sl], a.ring_prec);
-                }
-            }
-        }
-    }
-    if (a.ring_prec && a.ring_mode == 1) {
-        bits = __reduce_max_sync(0xffffffffu, bits);
-        if (lane == 0 && bits) atomicMax(a.amax + (long long)shot * a.slots + a.slot, bits);
     }
 }
 
