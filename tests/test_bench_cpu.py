@@ -43,7 +43,7 @@ def test_kernel_flags(argv, fwd, bwd):
 @pytest.mark.parametrize("argv,ring", [
     ([], "f16"),                             # multi-shot configuration
     (["--workload", "rvsp"], "f32"),         # FP32 throughout
-    (["--workload", "c5"], "bf16"),
+    (["--workload", "c5"], "i16"),
     (["--workload", "rvsp", "--ring", "f16"], "f16"),
 ])
 def test_ring_storage_per_workload(argv, ring):
