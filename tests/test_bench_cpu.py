@@ -81,3 +81,29 @@ def test_windowed_roofline_counts_every_shot_once_per_step(monkeypatch):
     assert r["frac"] == pytest.approx(r["achieved"] / 1000.0)
     assert r["launch_ms"] == pytest.approx(2.0) and r["pad_kernel_ms"] == pytest.approx(0.5)
     assert r["bound"] == "hbm" and r["unit"] == "GB/s"
+
+
+def test_reference_arm_runs_without_the_product_library(tmp_path):
+    """--impl reference on a small grid, in a fresh process: it prints the
+    product arm's config, times the reference's loop, and never maps the
+    product library (its problem comes from the oracle's restatement of the
+    reference's host code)."""
+    import json
+    import os
+    import subprocess
+    code = (
+        "import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--small', '--nt', '16',"
+        " '--steps', '1', '--warmup', '1']; import bench; bench.main();"
+        " maps = open('/proc/self/maps').read();"
+        " print(json.dumps({'product_mapped': 'librtm_gb300' in maps}))")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    line, maps = lines[0], lines[-1]
+    assert maps["product_mapped"] is False
+    assert line["impl"] == "reference" and line["value"] > 0 and line["steps"] == 1
+    assert line["config"] == bench.Config(_args("--small", "--nt", "16")).workload()
+    assert line["cpu_baseline"]["kind"] in ("reference", "port")
+    assert "reference_gpu" in line  # timed, or "unavailable" without a GPU
