@@ -210,13 +210,20 @@ int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb,
     }
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
+    eng::StepArgs la = a;
+    if (c->windowed) {
+        // narrowest grid among the launch's shots
+        int mn = c->NX;
+        for (int i = a.shot0; i < a.shot0 + nb && i < (int)c->hnx.size(); ++i) mn = std::min(mn, c->hnx[i]);
+        la.min_nx = mn;
+    }
     if (MODE == eng::MODE_FWD && (c->kv[MODE] == RTM_KERNEL_X2 || c->kv[MODE] == RTM_KERNEL_X2_SPLIT)) {
         eng::k_step_x2<MMAX, AD><<<grid, eng::X2_THREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
-                                                                     c->imaps, a);
+                                                                     c->imaps, la);
         return RTM_OK;
     }
     eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
-                                                                   c->imaps, a);
+                                                                   c->imaps, la);
     return RTM_OK;
 }
 
@@ -292,6 +299,7 @@ eng::StepArgs base_step(rtm_ctx *c)
     a.gbin_ss = c->windowed ? c->ss : 0;
     a.xas = c->gxa;
     a.gsbin = c->mbin;
+    a.min_nx = c->NX;
     return a;
 }
 

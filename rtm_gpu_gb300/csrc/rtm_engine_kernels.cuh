@@ -125,6 +125,10 @@ struct StepArgs {
     // survey) of each shot, and the survey's bins (same pitch P)
     const int *xas;
     const int *gsbin;
+    // narrowest padded width among the launch's shots: tiles starting left
+    // of it exist in every shot, so they issue their wavefield copies before
+    // reading the shot's own width and origin
+    int min_nx;
 };
 
 // Whether a tile of a windowed shot reads its model tiles from the survey's
@@ -293,26 +297,19 @@ __device__ __forceinline__ bool tile_has_interior_rows(int z0, int NZ, int N2)
     return z0 + TZ > N2 && z0 < NZ - N2;
 }
 
+// The copies of a tile except its model tiles (one arrive on `bar` with the
+// byte count of all of them, model tiles included).
 template <int MMAX, int MODE, bool ADAPT>
-__device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t *bar,
-                                           const CUtensorMap &mapA, const CUtensorMap &mapS,
-                                           const CUtensorMap &flatA0, const CUtensorMap &flatS0,
-                                           const ModelMaps &mod, const ImgMaps &img, int x0,
-                                           int z0, int shot, int vshot, bool with_s, bool surv = false,
-                                           int xa = 0)
+__device__ __forceinline__ void issue_fields(const Stage<MMAX, MODE> &st, uint64_t *bar,
+                                             const CUtensorMap &mapA, const CUtensorMap &mapS,
+                                             const CUtensorMap &flatA0, const CUtensorMap &flatS0,
+                                             const ImgMaps &img, int x0, int z0, int shot, bool with_s)
 {
     using S = Shape<MMAX>;
     const unsigned skip = (MODE == MODE_BWD && !with_s) ? S::BYTES + 5u * FLAT_BYTES : 0u;
     mbar_arrive_expect_tx(bar, stage_tx_bytes<MMAX, MODE, ADAPT>() - skip);
     tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
     tma_load_3d(st.fA0, &flatA0, x0, z0, shot, bar);
-    if (surv) {
-        tma_load_3d(st.fV, &mod.svv, x0 + xa, z0, 0, bar);
-        if (ADAPT) tma_load_3d(st.fB, &mod.sbin, x0 + xa, z0, 0, bar);
-    } else {
-        tma_load_3d(st.fV, &mod.vv, x0, z0, vshot ? shot : 0, bar);
-        if (ADAPT) tma_load_3d(st.fB, &mod.bin, x0, z0, vshot ? shot : 0, bar);
-    }
     if (MODE == MODE_BWD && with_s) {
         tma_load_3d(st.tS, &mapS, x0 - S::XH, z0 - S::ZH, shot, bar);
         tma_load_3d(st.fS0, &flatS0, x0, z0, shot, bar);
@@ -321,6 +318,33 @@ __device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t
         tma_load_3d(st.fSa, &img.sacc, x0, z0, shot, bar);
         tma_load_3d(st.fRa, &img.racc, x0, z0, shot, bar);
     }
+}
+
+// The model tiles of a tile (vv and, adaptive, the bin words): from the
+// survey grid (surv), the shot's own window copy, or the shared grid.
+template <int MMAX, int MODE, bool ADAPT>
+__device__ __forceinline__ void issue_model(const Stage<MMAX, MODE> &st, uint64_t *bar, const ModelMaps &mod,
+                                            int x0, int z0, int shot, int vshot, bool surv, int xa)
+{
+    if (surv) {
+        tma_load_3d(st.fV, &mod.svv, x0 + xa, z0, 0, bar);
+        if (ADAPT) tma_load_3d(st.fB, &mod.sbin, x0 + xa, z0, 0, bar);
+    } else {
+        tma_load_3d(st.fV, &mod.vv, x0, z0, vshot ? shot : 0, bar);
+        if (ADAPT) tma_load_3d(st.fB, &mod.bin, x0, z0, vshot ? shot : 0, bar);
+    }
+}
+
+template <int MMAX, int MODE, bool ADAPT>
+__device__ __forceinline__ void issue_tile(const Stage<MMAX, MODE> &st, uint64_t *bar,
+                                           const CUtensorMap &mapA, const CUtensorMap &mapS,
+                                           const CUtensorMap &flatA0, const CUtensorMap &flatS0,
+                                           const ModelMaps &mod, const ImgMaps &img, int x0,
+                                           int z0, int shot, int vshot, bool with_s, bool surv = false,
+                                           int xa = 0)
+{
+    issue_fields<MMAX, MODE, ADAPT>(st, bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s);
+    issue_model<MMAX, MODE, ADAPT>(st, bar, mod, x0, z0, shot, vshot, surv, xa);
 }
 
 // The update of one staged 128 x 16 tile (after its copies landed and the
@@ -560,19 +584,27 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     const Stage<MMAX, MODE> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
-    // the shot's width and window origin: loads only when shots have their
-    // own windows, so that nothing delays the tile's copies otherwise
-    const int NX = a.vshot ? a.nxs[shot] : a.NX;
-    const int xa = a.vshot ? a.xas[shot] : 0;
-    if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid
-    const bool surv = tile_on_survey(a, x0, NX, xa);
-
     const bool with_s = tile_has_interior_rows(z0, a.NZ, a.N2);
-    if (threadIdx.x == 0) {
+    // a tile every shot of the launch has issues its wavefield copies before
+    // anything else; the shot's width and window origin (loads only when
+    // shots have their own windows) arrive while those copies fly
+    const bool early = x0 < a.min_nx;
+    if (early && threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
-        issue_tile<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot, a.vshot,
-                                      with_s, surv, xa);
+        issue_fields<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s);
+    }
+    const int NX = a.vshot ? a.nxs[shot] : a.NX;
+    const int xa = a.vshot ? a.xas[shot] : 0;
+    if (x0 >= NX) return;  // tile beyond this shot's (narrower) grid (never an early tile)
+    const bool surv = tile_on_survey(a, x0, NX, xa);
+    if (threadIdx.x == 0) {
+        if (!early) {
+            mbar_init(&bar, 1);
+            fence_barrier_init();
+            issue_fields<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s);
+        }
+        issue_model<MMAX, MODE, ADAPT>(st, &bar, mod, x0, z0, shot, a.vshot, surv, xa);
     }
     // fixed coefficients: once per thread, while the copies are in flight;
     // the first rows' adaptive coefficients likewise (issued by every thread
@@ -646,15 +678,23 @@ __global__ void __launch_bounds__(X2_THREADS, RTM_X2_MINB)
     const Stage<MMAX, MODE_FWD> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE_FWD>());
     const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ, shot = blockIdx.z + a.shot0;
+    const bool early = x0 < a.min_nx;  // as in k_step
+    if (early && threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+        issue_fields<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, false);
+    }
     const int NX = a.vshot ? a.nxs[shot] : a.NX;
     const int xa = a.vshot ? a.xas[shot] : 0;
     if (x0 >= NX) return;
     const bool surv = tile_on_survey(a, x0, NX, xa);
     if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
-        issue_tile<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, mod, img, x0, z0, shot,
-                                          a.vshot, false, surv, xa);
+        if (!early) {
+            mbar_init(&bar, 1);
+            fence_barrier_init();
+            issue_fields<MMAX, MODE_FWD, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, false);
+        }
+        issue_model<MMAX, MODE_FWD, ADAPT>(st, &bar, mod, x0, z0, shot, a.vshot, surv, xa);
     }
     float cc[MMAX + 1];
 #pragma unroll
