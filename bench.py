@@ -93,6 +93,10 @@ def parse():
                     help="time steps of the one-shot CPU sample (0: %d, about 10 s on 16 cores)"
                          % CPU_SAMPLE_NT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--snap", type=int, default=0,
+                    help="multishot: source snapshots every SNAP steps instead of boundary rings "
+                         "(the backward run images at the snapshot steps; 0: the ring scheme)")
+    ap.add_argument("--snap-storage", default="f16", choices=["f32", "bf16", "f16", "i16"])
     ap.add_argument("--no-fp64-check", action="store_true",
                     help="skip the one-shot image check against the FP64 oracle")
     ap.add_argument("--small", action="store_true", help="reduced grid for quick checks")
@@ -130,6 +134,9 @@ class Config:
         # of FP64 over its 8000 steps; BF16 and FP16 rings do not, --ring bf16)
         self.ring = a.ring or {"multishot": "f16", "c1": "f32", "rvsp": "f32", "c5": "i16"}[a.workload]
         self.whitecoe = 1e-4
+        # source snapshots every `snap` steps (0: the ring scheme)
+        self.snap = getattr(a, "snap", 0) or 0
+        self.snap_storage = getattr(a, "snap_storage", "f16")
         # optimiser settings (the reference's parameter file: nthita=1000,
         # eps=1e-5, df=1; fmax = 2*f0)
         self.fmax, self.df, self.nthita, self.eps, self.nfdmin = 2 * self.f0, 1.0, 1000, 1e-5, 2
@@ -153,6 +160,12 @@ class Config:
         b = 4 if self.ring == "f32" else 2
         return self.NT * 2 * self.M * (self.nz + self.nx) * b
 
+    def snap_bytes(self):
+        """Snapshot bytes of one shot (source field, and its running sum in fp32)."""
+        b = 4 if self.snap_storage == "f32" else 2
+        pitch = (self.nx + self.N2 % 8 + 7) // 8 * 8
+        return (3 + (self.NT - 5) // self.snap) * self.nz * pitch * (b + 4)
+
     def workload(self):
         """The `config` of both arms' bench lines (identical by construction)."""
         if self.name == "c1":
@@ -160,6 +173,17 @@ class Config:
                     "coefficients, %d steps, 20 Hz source at (2,200), %d surface receivers, FP32 "
                     "throughout" % (self.nz, self.nx, self.h, self.M, self.coef, self.NT, self.nx))
             l2 = "L2 flushed between timed steps (a 512 MB buffer written)"
+        elif self.snap:
+            text = ("multi-shot RTM %dx%d interior, 30-cell hybrid ABC, M=%d %s coefficients, "
+                    "%d steps, %d surface shots, full-spread receivers, FP32 stencil/imaging, "
+                    "source snapshots every %d steps in %s, their running sums in FP32 (no rings, "
+                    "no source reconstruction: the "
+                    "backward run images at every %dth step with end-corrected weights), Kahan "
+                    "stack; Gcell-updates counted as for the ring scheme's migration of the same "
+                    "shots" % (self.nz, self.nx, self.M, self.coef, self.NT, self.nshot, self.snap,
+                               self.snap_storage.upper(), self.snap))
+            l2 = ("inputs larger than L2 (the %d shots' snapshots are %.1f GB)"
+                  % (self.nshot, self.nshot * self.snap_bytes() / 1e9))
         else:
             text = ("multi-shot RTM %dx%d interior, 30-cell hybrid ABC, M=%d %s coefficients, "
                     "%d steps, %d surface shots, full-spread receivers, FP32 stencil/imaging, %s "
@@ -169,7 +193,9 @@ class Config:
                   % (self.nshot, self.nshot * self.ring_bytes() / 1e9))
         return {"workload": text, "nz": self.nz, "nx": self.nx, "N2": self.N2, "M": self.M,
                 "nt": self.NT, "shots": self.nshot, "dx_m": self.h, "dt_s": self.tao,
-                "coefficients": self.coef, "ring_storage": self.ring, "l2": l2,
+                "coefficients": self.coef, "ring_storage": "none" if self.snap else self.ring,
+                "snapshots": {"every": self.snap, "storage": self.snap_storage} if self.snap else None,
+                "l2": l2,
                 "reference_timing": "the reference arm times one shot of this grid over a "
                                     "prefix of its time steps and reports that sample's rate"}
 
@@ -744,10 +770,14 @@ def step_gathers(Engine, ptrue, pmig, src, batch, stream_handle, torch):
     return seis
 
 
-def ring_flag(cfg):
+def storage_flag(name):
     from rtm_gpu_gb300 import capi
     return {"f32": capi.RTM_RING_F32, "bf16": capi.RTM_RING_BF16, "f16": capi.RTM_RING_F16,
-            "i16": capi.RTM_RING_I16}[cfg.ring]
+            "i16": capi.RTM_RING_I16}[name]
+
+
+def ring_flag(cfg):
+    return storage_flag(cfg.ring)
 
 
 def run_multishot(a, cfg):
@@ -780,6 +810,8 @@ def run_multishot(a, cfg):
     seis = step_gathers(Engine, ptrue, pmig, src, batch, sh, torch)
 
     eng = Engine(pmig, batch=batch, stream=sh, ring_precision=ring_flag(cfg))
+    if cfg.snap:
+        eng.set_snapshots(cfg.snap, storage_flag(cfg.snap_storage))
     tuned = None
     if a.kernel == "auto":
         tuned = eng.autotune(src, nsteps=20)
@@ -862,15 +894,22 @@ def run_multishot(a, cfg):
     NZ, NX, nz, nx = pmig.NZ, pmig.NX, pmig.nz, pmig.nx
     bwd_bytes = nb * (16 * (NZ * NX + nz * nx) + 32 * nz * nx)
     fwd_bytes = nb * 16 * NZ * NX
+    bwd_kernel = "k_step<backward> (source reconstruction + receiver step + imaging)"
+    if cfg.snap:
+        # the receiver step on every cell and its running sum on the interior
+        # (the imaging at every snap-th step is a separate streaming kernel)
+        bwd_bytes = nb * (16 * NZ * NX + 8 * nz * nx)
+        fwd_bytes = nb * (16 * NZ * NX + 8 * nz * nx)  # plus the running sum's read and write
+        bwd_kernel = "k_step<backward, snapshots> (receiver step and its running sum)"
     bwd_ms = tm["bwd_ms"] / max(tm["bwd_n"], 1)
     fwd_ms = tm["fwd_ms"] / max(tm["fwd_n"], 1)
     peak, peak_kind = measured_peak()
-    traffic = measured_traffic(cfg, nb)
+    traffic = None if cfg.snap else measured_traffic(cfg, nb)
     achieved = bwd_bytes / (bwd_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": (traffic or {}).get("bytes"),
                 "traffic_source": (traffic or {}).get("source"),
-                "kernel": "k_step<backward> (source reconstruction + receiver step + imaging)",
+                "kernel": bwd_kernel,
                 "bytes_per_launch": bwd_bytes, "launch_ms": bwd_ms, "peak_kind": peak_kind,
                 "forward_kernel": {"launch_ms": fwd_ms, "bytes_per_launch": fwd_bytes,
                                    "achieved": fwd_bytes / (fwd_ms / 1e3) / 1e9},
@@ -891,8 +930,10 @@ def run_multishot(a, cfg):
         cpu = cpu_baseline(pmig, shots[0], seis_h[0].numpy(), nt_s, os.cpu_count() or 1)
     if rank == 0 and world == 1 and not a.no_fp64_check:
         i = nshot // 2
+        storage = ("source snapshots every %d steps in %s" % (cfg.snap, cfg.snap_storage.upper())
+                   if cfg.snap else "%s rings" % cfg.ring.upper())
         fp64 = fp64_check(eng, ptrue, pmig, shots[i], seis_h[i].numpy(), cfg.whitecoe,
-                          "shot %d of %d, %s rings, kernels as benched" % (i, nshot, cfg.ring.upper()))
+                          "shot %d of %d, %s, kernels as benched" % (i, nshot, storage))
 
     clocks = clk.summary(local)
     if rank == 0:
@@ -1038,9 +1079,10 @@ def main():
     a = parse()
     cfg = Config(a)
     if a.impl == "reference":
-        if a.workload in ("rvsp", "c5"):
+        if a.workload in ("rvsp", "c5") or a.snap:
             print(json.dumps({"impl": "reference", "unavailable":
-                              "the reference arm is defined for the multishot and c1 workloads"}))
+                              "the reference arm is defined for the multishot and c1 workloads "
+                              "with boundary rings (the reference stores no source snapshots)"}))
             return
         run_reference_arm(a, cfg)
         return

@@ -328,6 +328,36 @@ enum {
 int rtm_ctx_set_kernel(rtm_ctx *ctx, int fwd_variant, int bwd_variant, int shots_per_launch);
 int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
                        int *shots_per_launch);
+
+/* Source snapshots (no reference counterpart: the reference reconstructs the
+ * source field from its boundary rings at every backward step,
+ * kernel.cu:892-901).  With every = K > 0, a migration's forward run stores
+ * the source field's interior at steps 0, 1 (the start levels), 2, 2+K,
+ * 2+2K, .. <= NT-3 and, for
+ * compensated imaging, the running sum of the source field before each of
+ * those steps; the source field as RTM_RING_* storage (16-bit codes with one
+ * scale per shot and slot, the slot's max |value|; or fp32), the running sum
+ * as fp32 (it changes slowly from slot to slot, so its rounding would not
+ * average out and the image's Laplacian filter would show it); it saves no
+ * rings.
+ * Its backward run advances the receiver field alone (no source
+ * reconstruction) and applies the imaging condition at the snapshot steps
+ * only, each weighted by its share of the time sum (levels 0 and 1 with
+ * weight 1, the others by the trapezoidal rule with step K plus end
+ * corrections: every weight is 1 when K = 1), the source's running
+ * sum being the forward total minus the stored prefix.  The image therefore
+ * differs from the reference's per-step imaging by the time-sampling error
+ * and the storage rounding (measured: 3e-4 of the finished image against
+ * FP64 on a 201x401, 2000-step shot at K = 4; the time sampling aliases the
+ * broadband start-up content of larger grids).  Storage per shot:
+ * 3 + (NT-5)/K slots x nz x nx values of 2 or 4 bytes, plus as many of
+ * 4 bytes with compensated imaging.  every = 0 turns snapshots
+ * off (the default).  Returns RTM_ERR_NOMEM, snapshots off, when the device
+ * cannot hold them.  Snapshot steps always run the tiled stencil forms (one
+ * stream or the two halves); forms that do not exist for them fall back. */
+int rtm_ctx_set_snapshots(rtm_ctx *ctx, int every, int precision);
+/* Current snapshot setting and the device bytes of the stored snapshots. */
+int rtm_ctx_get_snapshots(const rtm_ctx *ctx, int *every, int *precision, size_t *bytes);
 /* Autotuner: times nsteps forward and nsteps backward time steps of the
  * first shots of a survey (optional windows as rtm_migrate_stack_windows)
  * for each kernel form (twice, interleaved, keeping each form's faster run)

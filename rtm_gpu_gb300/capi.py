@@ -16,6 +16,7 @@ from . import _build
 _lib = None
 
 RTM_OK = 0
+RTM_ERR_ARG, RTM_ERR_CUDA, RTM_ERR_NOMEM, RTM_ERR_DEVICE = -1, -2, -3, -4
 RTM_DEVICE_PTRS = 1
 RTM_NO_GRAPH = 2
 RTM_RING_F32, RTM_RING_BF16, RTM_RING_F16, RTM_RING_I16 = 0, 1, 2, 3
@@ -99,6 +100,8 @@ def lib():
         L.rtm_ctx_launches.argtypes = [vp, C.POINTER(C.c_long), I]
         L.rtm_ctx_set_kernel.argtypes = [vp, I, I, I]
         L.rtm_ctx_get_kernel.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.rtm_ctx_set_snapshots.argtypes = [vp, I, I]
+        L.rtm_ctx_get_snapshots.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_size_t)]
         L.rtm_ctx_autotune.argtypes = [vp, I, ip, ip, ip, I, C.POINTER(C.c_double)]
         L.rtm_resample.argtypes = [fp, I, I, C.c_float, fp, I, C.c_float, I]
         L.rtm_selftest_wait_timeout.argtypes = [C.c_uint, C.POINTER(C.c_uint)]

@@ -114,6 +114,19 @@ struct rtm_ctx {
     int4 *meta_s = nullptr;
     float4 *fac_s = nullptr;                      // [B][nabc] window pad tables
     eng::ImgMaps imaps;                // flat tiles of the imaging accumulators
+    // source snapshots (rtm_ctx_set_snapshots): every snap_every-th step
+    // (0: off) the forward run stores the source field's interior and its
+    // running sum (RTM_RING_* storage, per-(shot, slot) scales for 16-bit
+    // codes); the backward run then advances the receiver field alone and
+    // images at the snapshot steps
+    int snap_every = 0, snap_prec = 0, snap_nslots = 0, snap_off = 0, snap_pitch = 0;
+    void *snapS = nullptr;                      // [B][nslots][nz][snap_pitch] source field
+    float *snapQ = nullptr;                     // the same for its running sum (fp32)
+    float *pacc = nullptr;                      // [B][NZ][P] running sum of the source field
+    float *snap_scale = nullptr;                // [B][nslots] scale of the 16-bit codes
+    unsigned *snap_amax = nullptr;              // [B][nslots] max |S| (float bits)
+    size_t snap_bytes = 0;                      // device bytes of the above
+    eng::SnapMaps smaps_f{}, smaps_b{};         // running sums: pacc (forward), racc (backward)
     size_t bytes = 0;
     // graphs keyed by (phase, batch)
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
@@ -143,8 +156,21 @@ int dalloc(rtm_ctx *c, T **p, size_t n)
     return RTM_OK;
 }
 
+void free_snapshots(rtm_ctx *c)
+{
+    for (void *q : {c->snapS, (void *)c->snapQ, (void *)c->pacc, (void *)c->snap_scale, (void *)c->snap_amax})
+        if (q) cudaFree(q);
+    c->snapS = nullptr;
+    c->snapQ = c->pacc = c->snap_scale = nullptr;
+    c->snap_amax = nullptr;
+    c->snap_every = c->snap_nslots = 0;
+    c->bytes -= c->snap_bytes;
+    c->snap_bytes = 0;
+}
+
 void free_all(rtm_ctx *c)
 {
+    free_snapshots(c);
     if (c->st2) cudaStreamDestroy(c->st2);
     c->st2 = nullptr;
     for (cudaEvent_t *ev : {&c->evf[0], &c->evf[1], &c->evc[0], &c->evc[1]})
@@ -202,11 +228,15 @@ template <int MMAX, bool AD, int MODE>
 int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb, cudaStream_t st)
 {
     const eng::ModelMaps &fv = c->windowed ? c->mmaps_s : c->mmaps;
-    if (c->kv[MODE] == RTM_KERNEL_PERSISTENT) {
-        const unsigned smem = eng::PipeSmem<MMAX, MODE>::BYTES;
-        eng::k_step_pipe<MMAX, AD, MODE><<<pipe_grid<MMAX, AD, MODE>(), eng::NTHREADS, smem, c->st>>>(
-            *m.A, *m.S, *m.A0, *m.S0, fv, c->imaps, a, c->gitem, nb);
-        return RTM_OK;
+    constexpr int KI = eng::fwd_mode(MODE) ? 0 : 1;  // kernel-form slot of the step
+    // (the snapshot steps run in the tiled form, in one stream or two halves)
+    if constexpr (MODE == eng::MODE_FWD || MODE == eng::MODE_BWD) {
+        if (c->kv[KI] == RTM_KERNEL_PERSISTENT) {
+            const unsigned smem = eng::PipeSmem<MMAX, MODE>::BYTES;
+            eng::k_step_pipe<MMAX, AD, MODE><<<pipe_grid<MMAX, AD, MODE>(), eng::NTHREADS, smem, c->st>>>(
+                *m.A, *m.S, *m.A0, *m.S0, fv, c->imaps, a, c->gitem, nb);
+            return RTM_OK;
+        }
     }
     const unsigned smem = eng::Smem<MMAX, MODE>::BYTES;
     dim3 grid(cdiv(c->NX, eng::TX), cdiv(c->NZ, eng::TZ), nb);
@@ -217,13 +247,15 @@ int launch_step_t(rtm_ctx *c, const StepMaps &m, const eng::StepArgs &a, int nb,
         for (int i = a.shot0; i < a.shot0 + nb && i < (int)c->hnx.size(); ++i) mn = std::min(mn, c->hnx[i]);
         la.min_nx = mn;
     }
-    if (MODE == eng::MODE_FWD && (c->kv[MODE] == RTM_KERNEL_X2 || c->kv[MODE] == RTM_KERNEL_X2_SPLIT)) {
-        eng::k_step_x2<MMAX, AD><<<grid, eng::X2_THREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
-                                                                     c->imaps, la);
-        return RTM_OK;
+    if constexpr (MODE == eng::MODE_FWD) {
+        if (c->kv[KI] == RTM_KERNEL_X2 || c->kv[KI] == RTM_KERNEL_X2_SPLIT) {
+            eng::k_step_x2<MMAX, AD><<<grid, eng::X2_THREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
+                                                                         c->imaps, la);
+            return RTM_OK;
+        }
     }
-    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, st>>>(*m.A, *m.S, *m.A0, *m.S0, fv,
-                                                                   c->imaps, la);
+    eng::k_step<MMAX, AD, MODE><<<grid, eng::NTHREADS, smem, st>>>(
+        *m.A, *m.S, *m.A0, *m.S0, fv, c->imaps, MODE == eng::MODE_BWDS ? c->smaps_b : c->smaps_f, la);
     return RTM_OK;
 }
 
@@ -232,7 +264,8 @@ void set_attr_t()
 {
     const int smem = (int)eng::Smem<MMAX, MODE>::BYTES;
     cudaFuncSetAttribute(eng::k_step<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (MODE == eng::MODE_FWD)
+    if constexpr (MODE == eng::MODE_FWDS || MODE == eng::MODE_BWDS) return;
+    if constexpr (MODE == eng::MODE_FWD)
         cudaFuncSetAttribute(eng::k_step_x2<MMAX, AD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     const int psmem = (int)eng::PipeSmem<MMAX, MODE>::BYTES;
     cudaFuncSetAttribute(eng::k_step_pipe<MMAX, AD, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem);
@@ -250,6 +283,10 @@ void set_attr_m()
     set_attr_t<MMAX, false, eng::MODE_FWD>();
     set_attr_t<MMAX, true, eng::MODE_BWD>();
     set_attr_t<MMAX, false, eng::MODE_BWD>();
+    set_attr_t<MMAX, true, eng::MODE_FWDS>();
+    set_attr_t<MMAX, false, eng::MODE_FWDS>();
+    set_attr_t<MMAX, true, eng::MODE_BWDS>();
+    set_attr_t<MMAX, false, eng::MODE_BWDS>();
 }
 
 void init_step_attrs()
@@ -266,11 +303,20 @@ template <int MMAX>
 int launch_step_m(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb, cudaStream_t st)
 {
     const bool ad = c->p.adaptive != 0;
-    if (mode == eng::MODE_FWD)
+    switch (mode) {
+    case eng::MODE_FWD:
         return ad ? launch_step_t<MMAX, true, eng::MODE_FWD>(c, m, a, nb, st)
                   : launch_step_t<MMAX, false, eng::MODE_FWD>(c, m, a, nb, st);
-    return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, m, a, nb, st)
-              : launch_step_t<MMAX, false, eng::MODE_BWD>(c, m, a, nb, st);
+    case eng::MODE_BWD:
+        return ad ? launch_step_t<MMAX, true, eng::MODE_BWD>(c, m, a, nb, st)
+                  : launch_step_t<MMAX, false, eng::MODE_BWD>(c, m, a, nb, st);
+    case eng::MODE_FWDS:
+        return ad ? launch_step_t<MMAX, true, eng::MODE_FWDS>(c, m, a, nb, st)
+                  : launch_step_t<MMAX, false, eng::MODE_FWDS>(c, m, a, nb, st);
+    default:
+        return ad ? launch_step_t<MMAX, true, eng::MODE_BWDS>(c, m, a, nb, st)
+                  : launch_step_t<MMAX, false, eng::MODE_BWDS>(c, m, a, nb, st);
+    }
 }
 
 int launch_step(rtm_ctx *c, int mode, const StepMaps &m, const eng::StepArgs &a, int nb, cudaStream_t st)
@@ -301,6 +347,56 @@ eng::StepArgs base_step(rtm_ctx *c)
     a.gsbin = c->mbin;
     a.min_nx = c->NX;
     return a;
+}
+
+// Snapshot steps of a backward run over k = 0..N (N = NT-3) with snapshots
+// every K steps: the start levels 0 and 1 (level 1 is the start-up spike of a
+// single cell, level 0 is zero: both enter with weight 1), then k = 2, 2+K,
+// .., 2+KJ (J = (N-2) / K).  snap_slot gives the slot of a snapshot step (-1
+// at other steps); snap_weight the step's imaging weight in the time sum --
+// on the sampled steps the trapezoidal rule with step K, the rectangle sum's
+// end terms, the first end's derivative term of the Euler-Maclaurin formula
+// (the running sums are largest there) and the last sample standing for the
+// N-2-KJ steps above it.  The weights add up to N + 1; with K = 1 every
+// weight is 1.
+int snap_slot(int k, int K)
+{
+    if (k <= 1) return k;
+    return (k - 2) % K ? -1 : 2 + (k - 2) / K;
+}
+
+int snap_slots(int N, int K) { return 3 + (N - 2) / K; }
+
+double snap_weight(int k, int K, int N)
+{
+    if (k <= 1) return 1.0;
+    if ((k - 2) % K) return 0.0;
+    const int J = (N - 2) / K, j = (k - 2) / K;
+    if (J == 0) return N - 1.0;
+    const double e = (double(K) * K - 1.0) / (12.0 * K);
+    double w = K;
+    if (j == 0) w = (K + 1) / 2.0 - e;
+    if (j == J) w = (K + 1) / 2.0 + (N - 2 - K * J);
+    if (j == 1) w += e;
+    return w;
+}
+
+// Stores the snapshot of step k of n shots from the source level `lev` (its
+// interior; the running sum is c->pacc): max pass for 16-bit codes, then the
+// store.
+void snap_store(rtm_ctx *c, const float *lev, int k, int qzero, int shot0, int n, cudaStream_t st)
+{
+    const int slot = snap_slot(k, c->snap_every);
+    const dim3 grid(cdiv((long)c->nz * c->nx, 256), n);
+    if (c->snap_prec) {
+        eng::k_snap_max<<<grid, 256, 0, st>>>(lev, c->ss, c->NZ, c->P, c->N2, c->gnx, c->snap_amax,
+                                              c->snap_nslots, slot, shot0);
+        c->launches++;
+    }
+    eng::k_snap_store<<<grid, 256, 0, st>>>(lev, c->pacc, c->ss, c->NZ, c->P, c->N2, c->gnx, c->snap_amax,
+                                            c->snap_scale, c->snap_nslots, slot, qzero, c->snap_prec,
+                                            c->snap_pitch, c->snap_off, c->snapS, c->snapQ, shot0);
+    c->launches++;
 }
 
 eng::PadArgs base_pad(rtm_ctx *c)
@@ -390,11 +486,23 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     eng::k_shot_init<<<dim3(cdiv(ss, 256), nb), 256, 0, c->st>>>(c->S[0], c->S[1], c->S[2], c->pre,
                                                                  c->src, c->gnx, c->p.spike, ss, c->P);
     c->launches++;
-    const bool r16 = c->p.ring_precision != RTM_RING_F32;
+    // a migration with source snapshots saves no rings (its backward run
+    // does not reconstruct the source field)
+    const bool snap = c->snap_every > 0 && !rec_on;
+    const bool r16 = c->p.ring_precision != RTM_RING_F32 && !snap;
     const long long bstage = (long long)c->B * c->ringsz;  // floats of one stage parity
     if (r16 && c->M > 0)
         RTM_CUDA_TRY(cudaMemsetAsync(c->ramax, 0, sizeof(unsigned) * (size_t)c->B * NT, c->st));
-    if (c->M > 0) {
+    if (snap) {
+        // running sum of levels 0 and 1 (the start spike), and the slots of
+        // those two levels (level 0 is zero)
+        RTM_CUDA_TRY(cudaMemcpyAsync(c->pacc, c->S[1], sizeof(float) * (size_t)ss * nb, cudaMemcpyDeviceToDevice,
+                                     c->st));
+        RTM_CUDA_TRY(cudaMemsetAsync(c->snap_amax, 0, sizeof(unsigned) * (size_t)nb * c->snap_nslots, c->st));
+        snap_store(c, c->S[0], 0, 1, 0, nb, c->st);
+        snap_store(c, c->S[1], 1, 0, 0, nb, c->st);
+    }
+    if (c->M > 0 && !snap) {
         if (r16)
             eng::k_ring_fill<<<dim3(cdiv(abc_count(c->NZ, c->NX, c->N2), 256), nb), 256, 0, c->st>>>(
                 c->S[1], c->rstage + 1 * bstage, ss, c->ringsz, c->NZ, c->gnx, c->P, c->N2, c->M,
@@ -404,7 +512,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
                 c->S[1], c->ring + c->ringsz, ss, (long long)NT * c->ringsz, c->NZ, c->gnx, c->P, c->N2,
                 c->M, nullptr, 0);
     }
-    c->launches += (c->M > 0);
+    c->launches += (c->M > 0 && !snap);
     const long long rss = (long long)NT * c->nrec;
     if (rec_on && c->nrec > 0) {
         eng::k_record<<<dim3(cdiv(c->nrec, 128), nb), 128, 0, c->st>>>(
@@ -416,6 +524,8 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
     eng::PadArgs pa = base_pad(c);
     const long extra = (rec_on ? c->nrec : 0) + (r16 ? c->ringsz : 0);
     const int kend = c->kstop ? std::min(c->kstop, NT) : NT;  // kstop-2 steps when tuning
+    const int mode = snap ? eng::MODE_FWDS : eng::MODE_FWD;
+    if (snap) sa.pacc = c->pacc;
     Half hv[2];
     const int nh = halves(c, eng::MODE_FWD, nb, hv);
     for (int k = 2; k < kend; ++k) {
@@ -425,7 +535,7 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         const StepMaps sm{&c->mapS[(k - 1) % 3], &c->mapS[(k - 1) % 3], &c->flatS[(k - 2) % 3],
                           &c->flatS[(k - 2) % 3]};
         pa.a0 = a0; pa.a1 = a1; pa.a2 = a2;
-        pa.ring_mode = c->M > 0 ? 1 : 0;
+        pa.ring_mode = c->M > 0 && !snap ? 1 : 0;
         pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
         if (r16) {
             pa.slot = k;
@@ -438,11 +548,13 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         for (int h = 0; h < nh; ++h) {
             sa.shot0 = pa.shot0 = hv[h].shot0;
             tic(c);
-            if (int rc = launch_step(c, eng::MODE_FWD, sm, sa, hv[h].n, hv[h].st)) return rc;
+            if (int rc = launch_step(c, mode, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 0);
             tic(c);
             launch_pad(c, pa, hv[h].n, extra, hv[h].st);
             toc(c, 2);
+            if (snap && k <= NT - 3 && snap_slot(k, c->snap_every) >= 0)  // the backward run images k <= NT-3
+                snap_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
         }
     }
     join(c, nh);
@@ -472,6 +584,8 @@ int enqueue_backward(rtm_ctx *c, int nb)
     sa.dstride = (long long)NT * c->nrec;
     eng::PadArgs pa = base_pad(c);
     const int kend = c->kstop ? std::max(NT - c->kstop, 0) : 0;  // kstop-2 steps when tuning
+    const bool snap = c->snap_every > 0;
+    const int mode = snap ? eng::MODE_BWDS : eng::MODE_BWD;
     Half hv[2];
     const int nh = halves(c, eng::MODE_BWD, nb, hv);
     for (int k = NT - 3; k >= kend; --k) {
@@ -482,7 +596,9 @@ int enqueue_backward(rtm_ctx *c, int nb)
         sa.dinj = c->data + (long long)(k + 1) * c->nrec;
         const StepMaps sm{&c->mapR[i1], &c->mapS[i1], &c->flatR[i0], &c->flatS[i0]};
         pa.a0 = c->R[i0]; pa.a1 = c->R[i1]; pa.a2 = c->R[i2];
-        pa.ring_mode = c->M > 0 ? 2 : 0;
+        pa.ring_mode = c->M > 0 && !snap ? 2 : 0;
+        if (snap) sa.pacc = c->racc;
+        const float w = snap ? (float)snap_weight(k, c->snap_every, NT - 3) : 0.0f;
         pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
         pa.slot = k;
         pa.s2 = c->S[i2];
@@ -490,8 +606,15 @@ int enqueue_backward(rtm_ctx *c, int nb)
         for (int h = 0; h < nh; ++h) {
             sa.shot0 = pa.shot0 = hv[h].shot0;
             tic(c);
-            if (int rc = launch_step(c, eng::MODE_BWD, sm, sa, hv[h].n, hv[h].st)) return rc;
+            if (int rc = launch_step(c, mode, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 1);
+            if (w != 0.0f) {
+                eng::k_snap_image<<<dim3(cdiv((long)c->nz * c->nx, 256), hv[h].n), 256, 0, hv[h].st>>>(
+                    c->R[i2], c->racc, c->pacc, c->snapS, c->snapQ, c->snap_scale, c->rel1, c->rel2, c->ss,
+                    c->NZ, c->P, c->N2, c->gnx, c->snap_nslots, snap_slot(k, c->snap_every), c->snap_prec, c->snap_pitch,
+                    c->snap_off, w, c->p.compen, hv[h].shot0);
+                c->launches++;
+            }
             tic(c);
             launch_pad(c, pa, hv[h].n, 0, hv[h].st);
             toc(c, 2);
@@ -1019,6 +1142,67 @@ int rtm_ctx_set_kernel(rtm_ctx *c, int fwd_variant, int bwd_variant, int shots_p
     c->kv[0] = fwd_variant;
     c->kv[1] = bwd_variant;
     c->nbl = shots_per_launch ? shots_per_launch : c->B;
+    return RTM_OK;
+}
+
+int rtm_ctx_set_snapshots(rtm_ctx *c, int every, int precision)
+{
+    if (!c || every < 0 || precision < RTM_RING_F32 || precision > RTM_RING_I16) return RTM_ERR_ARG;
+    if (c->NT < 5 && every > 0) return RTM_ERR_ARG;
+    // the captured time loops change with the mode
+    for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    RTM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    free_snapshots(c);
+    if (every == 0) return RTM_OK;
+    const int nslots = snap_slots(c->NT - 3, every);  // steps 0, 1, 2, 2+K, .. <= NT-3
+    // column offset of the stored interior: a plane row from x0 - N2 + off =
+    // x0 - 8*floor(N2/8) on (x0 a multiple of 8) starts on 16 bytes
+    const int off = c->N2 % 8;
+    const int pitch = (c->nx + off + 7) / 8 * 8;
+    const size_t es = precision == RTM_RING_F32 ? 4 : 2;
+    const size_t plane = (size_t)c->nz * pitch;
+    const long long planes = (long long)c->B * nslots;
+    int rc = RTM_OK;
+    auto balloc = [&](void **q, size_t bytes) {
+        if (rc) return;
+        if (cudaMalloc(q, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            *q = nullptr;
+            rtm_set_last_error("cudaMalloc failed (source snapshots)");
+            rc = RTM_ERR_NOMEM;
+            return;
+        }
+        c->bytes += bytes;
+        c->snap_bytes += bytes;
+    };
+    balloc(&c->snapS, plane * planes * es);
+    if (c->p.compen) balloc(reinterpret_cast<void **>(&c->snapQ), plane * planes * sizeof(float));
+    balloc(reinterpret_cast<void **>(&c->pacc), sizeof(float) * (size_t)c->B * c->ss);
+    balloc(reinterpret_cast<void **>(&c->snap_scale), sizeof(float) * (size_t)planes);
+    balloc(reinterpret_cast<void **>(&c->snap_amax), sizeof(unsigned) * (size_t)planes);
+    if (!rc) {
+        c->snap_every = every;
+        c->snap_prec = precision;
+        c->snap_nslots = nslots;
+        c->snap_off = off;
+        c->snap_pitch = pitch;
+        rc = make_map(&c->smaps_f.sum, c->pacc, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ);
+        c->smaps_b.sum = c->imaps.racc;
+    }
+    if (rc) free_snapshots(c);
+    return rc;
+}
+
+int rtm_ctx_get_snapshots(const rtm_ctx *c, int *every, int *precision, size_t *bytes)
+{
+    if (!c) return RTM_ERR_ARG;
+    if (every) *every = c->snap_every;
+    if (precision) *precision = c->snap_prec;
+    if (bytes)
+        *bytes = c->snap_every ? (size_t)c->B * c->snap_nslots * c->nz * c->snap_pitch *
+                                     ((c->snap_prec ? 2 : 4) + (c->snapQ ? 4 : 0))
+                               : 0;
     return RTM_OK;
 }
 

@@ -63,16 +63,26 @@ struct Shape {
     static constexpr unsigned BYTES = ELEMS * 4u;
 };
 
+// Step kinds of k_step: the forward and backward steps of the ring scheme,
+// and the two steps of a migration with source snapshots: a forward step that
+// also accumulates the source field's running sum, and a backward step that
+// advances the receiver field alone (with its running sum; the imaging at the
+// snapshot steps is a separate streaming kernel, k_snap_image).
+enum { MODE_FWD = 0, MODE_BWD = 1, MODE_FWDS = 2, MODE_BWDS = 3 };
+__host__ __device__ constexpr bool fwd_mode(int m) { return m == MODE_FWD || m == MODE_FWDS; }
+
 // Shared-memory plan of k_step: halo boxes of the field(s) being advanced,
 // then flat tiles (u_{k-2} of each field, the per-cell factor v^2 tao^2/h^2,
 // the four imaging accumulators in the backward step, the per-cell velocity
 // bin), then the mbarrier.
 template <int MMAX, int MODE>
 struct Smem {
-    static constexpr int NBOX = MODE == 1 ? 2 : 1;
+    static constexpr int NBOX = MODE == MODE_BWD ? 2 : 1;
     // fwd: a0, vv, bin; bwd: a0, s0, vv, rel1, rel2, sacc, racc, bin (the bin
-    // tile is staged only with adaptive coefficients)
-    static constexpr int NFLAT = MODE == 1 ? 8 : 3;
+    // tile is staged only with adaptive coefficients); the snapshot steps:
+    // a0, vv, the running sum (source field forward, receiver field
+    // backward), bin
+    static constexpr int NFLAT = MODE == MODE_BWD ? 8 : (MODE == MODE_FWDS || MODE == MODE_BWDS) ? 4 : 3;
     static constexpr unsigned BYTES = NBOX * Shape<MMAX>::BYTES + NFLAT * FLAT_BYTES + 16u;
 };
 
@@ -88,7 +98,12 @@ struct ModelMaps {
     CUtensorMap vv, bin, svv, sbin;
 };
 
-enum { MODE_FWD = 0, MODE_BWD = 1 };
+// Flat tiles of the running sum of a migration with source snapshots (the
+// source field's in the forward run, the receiver field's in the backward
+// run; the [shot][NZ][P] layout of a field).
+struct SnapMaps {
+    CUtensorMap sum;
+};
 
 struct StepArgs {
     int NZ, NX, P, N2, nbins;
@@ -129,6 +144,10 @@ struct StepArgs {
     // of it exist in every shot, so they issue their wavefield copies before
     // reading the shot's own width and origin
     int min_nx;
+    // snapshot steps (MODE_FWDS / MODE_BWDS): the running sum the step adds
+    // its field's interior to (the source field's forward, the receiver
+    // field's backward with compensated imaging)
+    float *pacc;
 };
 
 // Whether a tile of a windowed shot reads its model tiles from the survey's
@@ -259,11 +278,38 @@ __device__ __forceinline__ float lap_cell(const float *q, int C, const float *ro
     return w1;
 }
 
+__host__ __device__ __forceinline__ float ring16_target(int prec) { return prec == 3 ? 32767.0f : 16384.0f; }
+
+// 16-bit ring codes: 1 BF16, 2 FP16 (floating point: relative rounding
+// 2^-9 / 2^-12 of each value), 3 int16 (a fixed-point fraction of the step's
+// largest value: absolute rounding of half of max/32767 for every value,
+// 16 times finer than FP16 at the largest values that dominate the field).
+__device__ __forceinline__ uint16_t ring_quant(float v, float inv, int prec)
+{
+    if (prec == 1) return __bfloat16_as_ushort(__float2bfloat16_rn(v * inv));
+    if (prec == 3) {
+        const int q = __float2int_rn(v * inv);  // |v| <= the step's max, so |q| <= 32767
+        return (uint16_t)(short)max(-32767, min(32767, q));
+    }
+    return __half_as_ushort(__float2half_rn(v * inv));
+}
+
+__device__ __forceinline__ float ring_dequant(uint16_t q, float sc, int prec)
+{
+    float f;
+    if (prec == 1) f = __bfloat162float(__ushort_as_bfloat16(q));
+    else if (prec == 3) f = (float)(short)q;
+    else f = __half2float(__ushort_as_half(q));
+    return f * sc;
+}
+
 // Shared-memory pointers of one pipeline stage (one tile's staged inputs).
 template <int MMAX, int MODE>
 struct Stage {
     float *tA, *tS, *fA0, *fV, *fS0, *fR1, *fR2, *fSa, *fRa;
     int *fB;
+    // snapshot steps: the running sum (in the slot of fS0)
+    float *fP;
     __device__ __forceinline__ explicit Stage(float *base)
     {
         using S = Shape<MMAX>;
@@ -273,6 +319,7 @@ struct Stage {
         fA0 = fl; fV = fl + FLAT;
         fS0 = fl + 2 * FLAT; fR1 = fl + 3 * FLAT; fR2 = fl + 4 * FLAT;
         fSa = fl + 5 * FLAT; fRa = fl + 6 * FLAT;
+        fP = fl + 2 * FLAT;
         fB = reinterpret_cast<int *>(fl + (Smem<MMAX, MODE>::NFLAT - 1) * FLAT);
     }
 };
@@ -303,9 +350,21 @@ template <int MMAX, int MODE, bool ADAPT>
 __device__ __forceinline__ void issue_fields(const Stage<MMAX, MODE> &st, uint64_t *bar,
                                              const CUtensorMap &mapA, const CUtensorMap &mapS,
                                              const CUtensorMap &flatA0, const CUtensorMap &flatS0,
-                                             const ImgMaps &img, int x0, int z0, int shot, bool with_s)
+                                             const ImgMaps &img, int x0, int z0, int shot, bool with_s,
+                                             const SnapMaps *snap = nullptr, const StepArgs *sa = nullptr)
 {
     using S = Shape<MMAX>;
+    if (MODE == MODE_FWDS || MODE == MODE_BWDS) {
+        // snapshot steps: the running sum's tile where the step adds to it
+        // (every forward tile; backward, tiles with interior rows when the
+        // imaging is compensated)
+        const bool sum = MODE == MODE_FWDS || (with_s && sa->compen);
+        mbar_arrive_expect_tx(bar, S::BYTES + (sum ? 3u : 2u) * FLAT_BYTES + (ADAPT ? FLAT_BYTES : 0u));
+        tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
+        tma_load_3d(st.fA0, &flatA0, x0, z0, shot, bar);
+        if (sum) tma_load_3d(st.fP, &snap->sum, x0, z0, shot, bar);
+        return;
+    }
     const unsigned skip = (MODE == MODE_BWD && !with_s) ? S::BYTES + 5u * FLAT_BYTES : 0u;
     mbar_arrive_expect_tx(bar, stage_tx_bytes<MMAX, MODE, ADAPT>() - skip);
     tma_load_3d(st.tA, &mapA, x0 - S::XH, z0 - S::ZH, shot, bar);
@@ -372,6 +431,27 @@ __device__ __forceinline__ void pre_gather(const StepArgs &a, const float *cc, i
     }
 }
 
+// Receiver injection of the backward steps: a receiver cell of the line
+// takes the step's recorded value where that is non-zero (kernel.cu's
+// Dirichlet injection of the observed data).
+__device__ __forceinline__ float inject_line(const StepArgs &a, float rv, int z, int gx, int rx0, int shot)
+{
+    int j = -1;
+    if (a.rdz == 0) {
+        if (z == a.rz0 && (gx - rx0) % a.rdx == 0) j = (gx - rx0) / a.rdx;
+    } else if (a.rdx == 0) {
+        if (gx == rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
+    } else if ((gx - rx0) % a.rdx == 0) {
+        const int jj = (gx - rx0) / a.rdx;
+        if (z == a.rz0 + jj * a.rdz) j = jj;
+    }
+    if (j >= 0 && j < a.nrec) {
+        const float d = a.dinj[(long long)shot * a.dstride + j];
+        if (d != 0.0f) rv = d;
+    }
+    return rv;
+}
+
 template <int MMAX, bool ADAPT, int MODE, int PF, int PRE>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX, MODE> &st,
                                              const float *cc, int x0, int z0, int shot, int NX,
@@ -417,8 +497,18 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
 #pragma unroll
     for (int i = PRE; i < PF; ++i) lr[i] = load_coefs<MMAX, ADAPT>(a, ADAPT ? fB[fr + i * TX] : 0, cc, cfr[i]);
 
-    if (MODE == MODE_FWD) {
-        // two rows per iteration: two independent accumulation chains
+    bool line_hit = false;
+    if (!fwd_mode(MODE) && a.nrec > 0) {
+        const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = rx0 + (a.nrec - 1) * a.rdx;
+        const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(rx0, xb), xhi = max(rx0, xb);
+        line_hit = !(zhi < zw || zlo >= zw + RW || xhi < x0 + wx * 32 || xlo >= x0 + wx * 32 + 32);
+    }
+    if (fwd_mode(MODE) || MODE == MODE_BWDS) {
+        // One field (forward: the source field; backward with snapshots: the
+        // receiver field, injected at the receivers), two rows per iteration:
+        // two independent accumulation chains.  The snapshot steps also add
+        // the field's interior to its running sum.
+        const bool sum = MODE == MODE_FWDS || (MODE == MODE_BWDS && a.compen);
         float q[QN + 1];
 #pragma unroll
         for (int j = 0; j < QN - 1; ++j) q[j] = tA[(rbase + j) * S::BW + cx];
@@ -441,13 +531,19 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
                 const int L = warp_len<MMAX, ADAPT>(lr[i + h]);
                 const float w1 = lap_cell<MMAX, ADAPT>(q, MMAX + h, row, cf, a.k0, a.hzx2_1, L);
                 float val = fmaf(fV[t], w1, 2.0f * q[MMAX + h] - fA0[t]);
-                if (i + h == src_row) val += a.wavelet;
+                if (fwd_mode(MODE)) {
+                    if (i + h == src_row) val += a.wavelet;
+                } else if (line_hit) {
+                    val = inject_line(a, val, z, gx, rx0, shot);
+                }
                 const long long g = g0 + (long)(i + h) * a.P;
                 if (inner) {
                     a.a2[g] = val;
+                    if (sum) a.pacc[g] = st.fP[t] + val;
                 } else if (col_ok) {
                     const bool interior = col_in && z >= N2 && z < NZ - N2;
                     if (interior) a.a2[g] = val;
+                    if (sum && interior) a.pacc[g] = st.fP[t] + val;
                     if (!interior || gx == N2 || gx == NX - 1 - N2 || z == N2 || z == NZ - 1 - N2)
                         a.pre[g] = val;
                 }
@@ -461,12 +557,6 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
     // Backward: receiver field R on every cell, reconstructed source field S
     // on the interior, advanced in lockstep so both share the coefficients and
     // the imaging condition sees both at once.
-    bool line_hit = false;
-    if (a.nrec > 0) {
-        const int zb = a.rz0 + (a.nrec - 1) * a.rdz, xb = rx0 + (a.nrec - 1) * a.rdx;
-        const int zlo = min(a.rz0, zb), zhi = max(a.rz0, zb), xlo = min(rx0, xb), xhi = max(rx0, xb);
-        line_hit = !(zhi < zw || zlo >= zw + RW || xhi < x0 + wx * 32 || xlo >= x0 + wx * 32 + 32);
-    }
     const bool rows_s = (zw + RW > N2) && (zw < NZ - N2);
     float qr[QN], qs[QN];
 #pragma unroll
@@ -500,21 +590,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage<MMAX
                     ws = fmaf(cl, (qs[MMAX - l] + qs[MMAX + l]) * a.hzx2_1 + rowS[-l] + rowS[l], ws);
             }
             float rv = fmaf(vv, wr, 2.0f * qr[MMAX] - fA0[t]);
-            if (line_hit) {
-                int j = -1;
-                if (a.rdz == 0) {
-                    if (z == a.rz0 && (gx - rx0) % a.rdx == 0) j = (gx - rx0) / a.rdx;
-                } else if (a.rdx == 0) {
-                    if (gx == rx0 && (z - a.rz0) % a.rdz == 0) j = (z - a.rz0) / a.rdz;
-                } else if ((gx - rx0) % a.rdx == 0) {
-                    const int jj = (gx - rx0) / a.rdx;
-                    if (z == a.rz0 + jj * a.rdz) j = jj;
-                }
-                if (j >= 0 && j < a.nrec) {
-                    const float d = a.dinj[(long long)shot * a.dstride + j];
-                    if (d != 0.0f) rv = d;
-                }
-            }
+            if (line_hit) rv = inject_line(a, rv, z, gx, rx0, shot);
             const bool interior = inner || (col_in && z >= N2 && z < NZ - N2);
             const long long g = g0 + (long)i * a.P;
             if (inner) {
@@ -576,10 +652,10 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     k_step(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapS,
            const __grid_constant__ CUtensorMap flatA0, const __grid_constant__ CUtensorMap flatS0,
            const __grid_constant__ ModelMaps mod, const __grid_constant__ ImgMaps img,
-           const StepArgs a)
+           const __grid_constant__ SnapMaps snap, const StepArgs a)
 {
     using SM = Smem<MMAX, MODE>;
-    constexpr int PF = MODE == MODE_FWD ? RTM_FWD_PF : (MMAX <= 8 ? RTM_BWD_PF : 2);  // register budget
+    constexpr int PF = MODE != MODE_BWD ? RTM_FWD_PF : (MMAX <= 8 ? RTM_BWD_PF : 2);  // register budget
     extern __shared__ __align__(128) float smem[];
     const Stage<MMAX, MODE> st(smem);
     uint64_t &bar = *reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + stage_bytes<MMAX, MODE>());
@@ -592,7 +668,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     if (early && threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_barrier_init();
-        issue_fields<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s);
+        issue_fields<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s, &snap, &a);
     }
     const int NX = a.vshot ? a.nxs[shot] : a.NX;
     const int xa = a.vshot ? a.xas[shot] : 0;
@@ -602,7 +678,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
         if (!early) {
             mbar_init(&bar, 1);
             fence_barrier_init();
-            issue_fields<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s);
+            issue_fields<MMAX, MODE, ADAPT>(st, &bar, mapA, mapS, flatA0, flatS0, img, x0, z0, shot, with_s, &snap, &a);
         }
         issue_model<MMAX, MODE, ADAPT>(st, &bar, mod, x0, z0, shot, a.vshot, surv, xa);
     }
@@ -618,7 +694,7 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD || MMAX > 8 ? 2 : R
     float cpre[PRE > 0 ? PRE : 1][MMAX + 1];
     int lpre[PRE > 0 ? PRE : 1];
     pre_gather<MMAX, ADAPT, PRE>(a, cc, x0, z0, shot, NX, cpre, lpre, surv, xa);
-    const int src = __ldg(a.src + shot), rx0 = MODE == MODE_BWD ? __ldg(a.rx0s + shot) : 0;
+    const int src = __ldg(a.src + shot), rx0 = !fwd_mode(MODE) ? __ldg(a.rx0s + shot) : 0;
     __syncthreads();  // the barrier is initialised before any thread waits on it
     const bool ok = mbar_wait_bounded(&bar, 0, &g_rtm_dev_error);
     if (tile_at_edge<MMAX>(x0, z0, NX, a.NZ)) {
@@ -969,29 +1045,79 @@ struct PadArgs {
 // Value a step's max |ring value| maps to: 16384 for FP16 / BF16 (FP16 keeps
 // headroom below 65504; BF16 uses the same scale), 32767 for the scaled
 // integers of RTM_RING_I16, whose values then fill the int16 range.
-__host__ __device__ __forceinline__ float ring16_target(int prec) { return prec == 3 ? 32767.0f : 16384.0f; }
-
-// 16-bit ring codes: 1 BF16, 2 FP16 (floating point: relative rounding
-// 2^-9 / 2^-12 of each value), 3 int16 (a fixed-point fraction of the step's
-// largest value: absolute rounding of half of max/32767 for every value,
-// 16 times finer than FP16 at the largest values that dominate the field).
-__device__ __forceinline__ uint16_t ring_quant(float v, float inv, int prec)
+// Source snapshots.  At a snapshot step of the forward run, S is the step's
+// source field and P its running sum after the step, so P - S is the sum of
+// the levels before the step.  A slot holds both over the shot's interior
+// (qzero: the slot of level 0, whose sum is zero) at plane shot*nslots+slot,
+// row z - N2, column x - N2 + off: S as fp32 or as 16-bit codes, fractions
+// of the slot's largest |S| (as the rings' codes); the running sum always as
+// fp32 -- it changes slowly from slot to slot, so 16-bit rounding of it would
+// repeat over many slots instead of averaging out, and the image's Laplacian
+// filter would bring that cell-to-cell noise out (FP16: 3e-3 of the image).
+__global__ void k_snap_max(const float *S, long long ss, int NZ, int P, int N2, const int *nxs,
+                           unsigned *amax, int nslots, int slot, int shot0)
 {
-    if (prec == 1) return __bfloat16_as_ushort(__float2bfloat16_rn(v * inv));
-    if (prec == 3) {
-        const int q = __float2int_rn(v * inv);  // |v| <= the step's max, so |q| <= 32767
-        return (uint16_t)(short)max(-32767, min(32767, q));
+    const int shot = blockIdx.y + shot0;
+    const int nx = nxs[shot] - 2 * N2, nz = NZ - 2 * N2;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned bs = 0;
+    if (i < (long long)nz * nx) {
+        const int z = N2 + (int)(i / nx), x = N2 + (int)(i % nx);
+        bs = __float_as_uint(fabsf(S[(long long)shot * ss + (long long)z * P + x]));
     }
-    return __half_as_ushort(__float2half_rn(v * inv));
+    bs = __reduce_max_sync(0xffffffffu, bs);
+    if ((threadIdx.x & 31) == 0 && bs) atomicMax(amax + (long long)shot * nslots + slot, bs);
 }
 
-__device__ __forceinline__ float ring_dequant(uint16_t q, float sc, int prec)
+__global__ void k_snap_store(const float *S, const float *pacc, long long ss, int NZ, int P, int N2,
+                             const int *nxs, const unsigned *amax, float *scale, int nslots, int slot,
+                             int qzero, int prec, int pitch, int off, void *outS, float *outQ, int shot0)
 {
-    float f;
-    if (prec == 1) f = __bfloat162float(__ushort_as_bfloat16(q));
-    else if (prec == 3) f = (float)(short)q;
-    else f = __half2float(__ushort_as_half(q));
-    return f * sc;
+    const int shot = blockIdx.y + shot0;
+    const int nx = nxs[shot] - 2 * N2, nz = NZ - 2 * N2;
+    const long long sl = (long long)shot * nslots + slot;
+    float inv = 1.0f;
+    if (prec) {
+        const float tgt = ring16_target(prec);
+        const float ms = __uint_as_float(amax[sl]);
+        inv = ms > 0.0f ? tgt / ms : 0.0f;
+        if (blockIdx.x == 0 && threadIdx.x == 0) scale[sl] = ms / tgt;
+    }
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nz * nx) return;
+    const int z = N2 + (int)(i / nx), x = N2 + (int)(i % nx);
+    const long long g = (long long)shot * ss + (long long)z * P + x;
+    const float sv = S[g];
+    const long long o = (sl * nz + (z - N2)) * pitch + (x - N2 + off);
+    if (prec == 0) static_cast<float *>(outS)[o] = sv;
+    else static_cast<uint16_t *>(outS)[o] = ring_quant(sv, inv, prec);
+    if (outQ) outQ[o] = qzero ? 0.0f : pacc[g] - sv;
+}
+
+// Imaging at snapshot step k of the backward run, over the interior of the
+// launch's shots (a streaming pass after the step's stencil): with the
+// stored source field S(k) and, compensated, the source's running sum
+// Tot - P_k (Tot: the forward run's total, P_k: the stored prefix) times the
+// receiver field's running sum, or, plain, the receiver field R(k) itself;
+// w is the step's share of the time sum (kernel.cu:489-517's accumulations).
+__global__ void k_snap_image(const float *R, const float *racc, const float *tot, const void *snapS,
+                             const float *snapQ, const float *scale, float *rel1, float *rel2, long long ss,
+                             int NZ, int P, int N2, const int *nxs, int nslots, int slot, int prec, int pitch,
+                             int off, float w, int compen, int shot0)
+{
+    const int shot = blockIdx.y + shot0;
+    const int nx = nxs[shot] - 2 * N2, nz = NZ - 2 * N2;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nz * nx) return;
+    const int z = N2 + (int)(i / nx), x = N2 + (int)(i % nx);
+    const long long g = (long long)shot * ss + (long long)z * P + x;
+    const long long sl = (long long)shot * nslots + slot;
+    const long long o = (sl * nz + (z - N2)) * pitch + (x - N2 + off);
+    const float sv = prec == 0 ? static_cast<const float *>(snapS)[o]
+                               : ring_dequant(static_cast<const uint16_t *>(snapS)[o], __ldg(scale + sl), prec);
+    if (compen) rel1[g] = fmaf(w, racc[g] * (tot[g] - snapQ[o]), rel1[g]);
+    else rel1[g] = fmaf(w, R[g] * sv, rel1[g]);
+    rel2[g] = fmaf(w, sv * sv, rel2[g]);
 }
 
 enum { PAD_ROWEDGE = 0, PAD_COLEDGE = 1, PAD_CORNER = 2 };

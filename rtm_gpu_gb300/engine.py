@@ -73,6 +73,18 @@ class Engine:
                    "get_kernel")
         return {"fwd": f.value, "bwd": b.value, "shots_per_launch": n.value}
 
+    def set_snapshots(self, every: int, precision: int = capi.RTM_RING_F16):
+        """Source snapshots every `every` steps (0: off) in RTM_RING_* storage:
+        the backward run then advances the receiver field alone and images at
+        the snapshot steps (rtm_ctx_set_snapshots)."""
+        capi.check(capi.lib().rtm_ctx_set_snapshots(self._h, int(every), int(precision)), "set_snapshots")
+
+    def snapshots(self):
+        e, p, b = C.c_int(), C.c_int(), C.c_size_t()
+        capi.check(capi.lib().rtm_ctx_get_snapshots(self._h, C.byref(e), C.byref(p), C.byref(b)),
+                   "get_snapshots")
+        return {"every": e.value, "precision": p.value, "bytes": b.value}
+
     def autotune(self, src_cells, win_x0=None, win_nx=None, nsteps: int = 20) -> float:
         """Times the kernel forms and shots per launch on the first shots of
         a survey, keeps the fastest; returns its Gcell-updates/s."""
