@@ -164,7 +164,9 @@ class Config:
         """Snapshot bytes of one shot (source field, and its running sum in fp32)."""
         b = 4 if self.snap_storage == "f32" else 2
         pitch = (self.nx + self.N2 % 8 + 7) // 8 * 8
-        return (3 + (self.NT - 5) // self.snap) * self.nz * pitch * (b + 4)
+        rows = (self.N2 + 1 + 24) - self.N2 + 1  # surface receiver line: rows N2 .. N2+1+24
+        band = rows * (self.nx - 1 + 2 * 24 + 1) * (self.NT - 2) * 8  # imaged every step, fp32
+        return (3 + (self.NT - 5) // self.snap) * self.nz * pitch * (b + 4) + band
 
     def workload(self):
         """The `config` of both arms' bench lines (identical by construction)."""
@@ -802,7 +804,9 @@ def run_multishot(a, cfg):
         from rtm_gpu_gb300.shard import shard_shots
         survey = synth.surface_shots(cfg.nx, nshot * world, cfg.N2)
         shots = [survey[i] for i in shard_shots(len(survey), rank, world)]
-    batch = a.batch or nshot
+    # with snapshots, 32 shots per batch (their snapshots, 2 GB per shot
+    # here, and the receiver band's every-step copies fit the device)
+    batch = a.batch or (min(nshot, 32) if cfg.snap else nshot)
     src = [pmig.src_flat(z, x) for z, x in shots]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)

@@ -345,13 +345,17 @@ int rtm_ctx_get_kernel(const rtm_ctx *ctx, int *fwd_variant, int *bwd_variant,
  * only, each weighted by its share of the time sum (levels 0 and 1 with
  * weight 1, the others by the trapezoidal rule with step K plus end
  * corrections: every weight is 1 when K = 1), the source's running
- * sum being the forward total minus the stored prefix.  The image therefore
- * differs from the reference's per-step imaging by the time-sampling error
- * and the storage rounding (measured: 3e-4 of the finished image against
- * FP64 on a 201x401, 2000-step shot at K = 4; the time sampling aliases the
- * broadband start-up content of larger grids).  Storage per shot:
- * 3 + (NT-5)/K slots x nz x nx values of 2 or 4 bytes, plus as many of
- * 4 bytes with compensated imaging.  every = 0 turns snapshots
+ * sum being the forward total minus the stored prefix -- except on the band
+ * of cells within 24 of the receiver line, where the receiver field is held
+ * to the recorded data, whose content reaches far above the sampled steps'
+ * rate: those cells are stored (fp32) and imaged at every step.  The image
+ * therefore differs from the reference's per-step imaging by the remaining
+ * time-sampling error and the storage rounding (measured at K = 4 against
+ * FP64: 1.4e-4 of the finished image on a 201x401, 2000-step shot, 5.7e-4
+ * on a 401x1201, 4000-step shot whose ring-scheme image is 5.5e-4 away).
+ * Storage per shot: 3 + (NT-5)/K slots x nz x nx values of 2 or 4 bytes,
+ * plus as many of 4 bytes with compensated imaging, plus the band's cells at
+ * NT-2 steps in 4 bytes (8 compensated).  every = 0 turns snapshots
  * off (the default).  Returns RTM_ERR_NOMEM, snapshots off, when the device
  * cannot hold them.  Snapshot steps always run the tiled stencil forms (one
  * stream or the two halves); forms that do not exist for them fall back. */

@@ -125,6 +125,10 @@ struct rtm_ctx {
     float *pacc = nullptr;                      // [B][NZ][P] running sum of the source field
     float *snap_scale = nullptr;                // [B][nslots] scale of the 16-bit codes
     unsigned *snap_amax = nullptr;              // [B][nslots] max |S| (float bits)
+    // cells around the receiver line, imaged at every step: their source
+    // field and running sum at every step k <= NT-3 ([B][NT-2][zn*xn], fp32)
+    eng::SnapBand band{};
+    float *bandS = nullptr, *bandP = nullptr;
     size_t snap_bytes = 0;                      // device bytes of the above
     eng::SnapMaps smaps_f{}, smaps_b{};         // running sums: pacc (forward), racc (backward)
     size_t bytes = 0;
@@ -158,10 +162,12 @@ int dalloc(rtm_ctx *c, T **p, size_t n)
 
 void free_snapshots(rtm_ctx *c)
 {
-    for (void *q : {c->snapS, (void *)c->snapQ, (void *)c->pacc, (void *)c->snap_scale, (void *)c->snap_amax})
+    for (void *q : {c->snapS, (void *)c->snapQ, (void *)c->pacc, (void *)c->snap_scale, (void *)c->snap_amax,
+                    (void *)c->bandS, (void *)c->bandP})
         if (q) cudaFree(q);
     c->snapS = nullptr;
-    c->snapQ = c->pacc = c->snap_scale = nullptr;
+    c->snapQ = c->pacc = c->snap_scale = c->bandS = c->bandP = nullptr;
+    c->band = eng::SnapBand{};
     c->snap_amax = nullptr;
     c->snap_every = c->snap_nslots = 0;
     c->bytes -= c->snap_bytes;
@@ -381,6 +387,15 @@ double snap_weight(int k, int K, int N)
     return w;
 }
 
+// The receiver band's cells of step k (k <= NT-3) of n shots.
+void band_store(rtm_ctx *c, const float *lev, int k, int qzero, int shot0, int n, cudaStream_t st)
+{
+    if (!c->band.zn) return;
+    eng::k_band_store<<<dim3(cdiv((long)c->band.zn * c->band.xn, 256), n), 256, 0, st>>>(
+        lev, c->pacc, c->ss, c->P, c->N2, c->gnx, c->grx0, c->band, c->NT - 2, k, qzero, c->bandS, c->bandP, shot0);
+    c->launches++;
+}
+
 // Stores the snapshot of step k of n shots from the source level `lev` (its
 // interior; the running sum is c->pacc): max pass for 16-bit codes, then the
 // store.
@@ -393,6 +408,7 @@ void snap_store(rtm_ctx *c, const float *lev, int k, int qzero, int shot0, int n
                                               c->snap_nslots, slot, shot0);
         c->launches++;
     }
+    band_store(c, lev, k, qzero, shot0, n, st);
     eng::k_snap_store<<<grid, 256, 0, st>>>(lev, c->pacc, c->ss, c->NZ, c->P, c->N2, c->gnx, c->snap_amax,
                                             c->snap_scale, c->snap_nslots, slot, qzero, c->snap_prec,
                                             c->snap_pitch, c->snap_off, c->snapS, c->snapQ, shot0);
@@ -553,8 +569,10 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
             tic(c);
             launch_pad(c, pa, hv[h].n, extra, hv[h].st);
             toc(c, 2);
-            if (snap && k <= NT - 3 && snap_slot(k, c->snap_every) >= 0)  // the backward run images k <= NT-3
-                snap_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
+            if (snap && k <= NT - 3) {  // the backward run images k <= NT-3
+                if (snap_slot(k, c->snap_every) >= 0) snap_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
+                else band_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
+            }
         }
     }
     join(c, nh);
@@ -608,11 +626,17 @@ int enqueue_backward(rtm_ctx *c, int nb)
             tic(c);
             if (int rc = launch_step(c, mode, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 1);
+            if (snap && c->band.zn) {
+                eng::k_band_image<<<dim3(cdiv((long)c->band.zn * c->band.xn, 256), hv[h].n), 256, 0, hv[h].st>>>(
+                    c->R[i2], c->racc, c->pacc, c->bandS, c->bandP, c->rel1, c->rel2, c->ss, c->P, c->N2, c->gnx,
+                    c->grx0, c->band, NT - 2, k, c->p.compen, hv[h].shot0);
+                c->launches++;
+            }
             if (w != 0.0f) {
                 eng::k_snap_image<<<dim3(cdiv((long)c->nz * c->nx, 256), hv[h].n), 256, 0, hv[h].st>>>(
                     c->R[i2], c->racc, c->pacc, c->snapS, c->snapQ, c->snap_scale, c->rel1, c->rel2, c->ss,
-                    c->NZ, c->P, c->N2, c->gnx, c->snap_nslots, snap_slot(k, c->snap_every), c->snap_prec, c->snap_pitch,
-                    c->snap_off, w, c->p.compen, hv[h].shot0);
+                    c->NZ, c->P, c->N2, c->gnx, c->grx0, c->band, c->snap_nslots, snap_slot(k, c->snap_every),
+                    c->snap_prec, c->snap_pitch, c->snap_off, w, c->p.compen, hv[h].shot0);
                 c->launches++;
             }
             tic(c);
@@ -1181,12 +1205,30 @@ int rtm_ctx_set_snapshots(rtm_ctx *c, int every, int precision)
     balloc(reinterpret_cast<void **>(&c->pacc), sizeof(float) * (size_t)c->B * c->ss);
     balloc(reinterpret_cast<void **>(&c->snap_scale), sizeof(float) * (size_t)planes);
     balloc(reinterpret_cast<void **>(&c->snap_amax), sizeof(unsigned) * (size_t)planes);
+    // receiver band: SNAP_BAND cells on each side of the receiver line
+    eng::SnapBand b{};
+    if (c->nrec > 0) {
+        constexpr int SNAP_BAND = 24;
+        const int zl = std::min(c->p.rz0, c->p.rz0 + (c->nrec - 1) * c->p.rdz);
+        const int zh = std::max(c->p.rz0, c->p.rz0 + (c->nrec - 1) * c->p.rdz);
+        const int xl = std::min(0, (c->nrec - 1) * c->p.rdx), xh = std::max(0, (c->nrec - 1) * c->p.rdx);
+        b.z0 = std::max(c->N2, zl - SNAP_BAND);
+        b.zn = std::max(0, std::min(c->NZ - c->N2 - 1, zh + SNAP_BAND) - b.z0 + 1);
+        b.xoff = xl - SNAP_BAND;
+        b.xn = xh - xl + 2 * SNAP_BAND + 1;
+    }
+    if (b.zn) {
+        const size_t bcells = (size_t)c->B * (c->NT - 2) * b.zn * b.xn;
+        balloc(reinterpret_cast<void **>(&c->bandS), sizeof(float) * bcells);
+        if (c->p.compen) balloc(reinterpret_cast<void **>(&c->bandP), sizeof(float) * bcells);
+    }
     if (!rc) {
         c->snap_every = every;
         c->snap_prec = precision;
         c->snap_nslots = nslots;
         c->snap_off = off;
         c->snap_pitch = pitch;
+        c->band = b;
         rc = make_map(&c->smaps_f.sum, c->pacc, c->NX, c->NZ, c->B, c->P, eng::TX, eng::TZ);
         c->smaps_b.sum = c->imaps.racc;
     }
@@ -1201,7 +1243,9 @@ int rtm_ctx_get_snapshots(const rtm_ctx *c, int *every, int *precision, size_t *
     if (precision) *precision = c->snap_prec;
     if (bytes)
         *bytes = c->snap_every ? (size_t)c->B * c->snap_nslots * c->nz * c->snap_pitch *
-                                     ((c->snap_prec ? 2 : 4) + (c->snapQ ? 4 : 0))
+                                         ((c->snap_prec ? 2 : 4) + (c->snapQ ? 4 : 0)) +
+                                     (size_t)c->B * (c->NT - 2) * c->band.zn * c->band.xn *
+                                         ((c->bandS ? 4 : 0) + (c->bandP ? 4 : 0))
                                : 0;
     return RTM_OK;
 }

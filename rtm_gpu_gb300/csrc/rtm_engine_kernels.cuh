@@ -1094,22 +1094,88 @@ __global__ void k_snap_store(const float *S, const float *pacc, long long ss, in
     if (outQ) outQ[o] = qzero ? 0.0f : pacc[g] - sv;
 }
 
+// The band of cells around a shot's receiver line that a migration with
+// snapshots images at every step (rows z0 .. z0+zn-1 of the padded grid,
+// inside the interior; xn columns from the shot's first receiver column plus
+// xoff, clipped to its interior).  There the receiver field is held to the
+// recorded data, whose content reaches far above the sampled steps' rate.
+struct SnapBand {
+    int z0, zn, xoff, xn;
+};
+
+__device__ __forceinline__ bool in_band(const SnapBand &b, int z, int x, int rx0)
+{
+    const int xb = x - (rx0 + b.xoff);
+    return z >= b.z0 && z < b.z0 + b.zn && xb >= 0 && xb < b.xn;
+}
+
+// Band cell i of a shot: its padded-grid row and column (false: outside the
+// shot's interior).
+__device__ __forceinline__ bool band_cell(const SnapBand &b, long long i, int rx0, int NX, int N2, int &z,
+                                          int &x)
+{
+    z = b.z0 + (int)(i / b.xn);
+    x = rx0 + b.xoff + (int)(i % b.xn);
+    return x >= N2 && x < NX - N2;
+}
+
+// Forward run, every step k <= NT-3: the band cells of the source field S(k)
+// and of its running sum before the step (qzero: level 0), fp32, at
+// [shot][k][cell].
+__global__ void k_band_store(const float *S, const float *pacc, long long ss, int P, int N2, const int *nxs,
+                             const int *rx0s, SnapBand b, int nsteps, int k, int qzero, float *bS, float *bP,
+                             int shot0)
+{
+    const int shot = blockIdx.y + shot0;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)b.zn * b.xn) return;
+    int z, x;
+    if (!band_cell(b, i, rx0s[shot], nxs[shot], N2, z, x)) return;
+    const long long g = (long long)shot * ss + (long long)z * P + x;
+    const long long o = ((long long)shot * nsteps + k) * b.zn * b.xn + i;
+    const float sv = S[g];
+    bS[o] = sv;
+    if (bP) bP[o] = qzero ? 0.0f : pacc[g] - sv;
+}
+
+// Backward run, every step k: the imaging condition on the band cells, as
+// the ring scheme applies it at every step (weight 1).
+__global__ void k_band_image(const float *R, const float *racc, const float *tot, const float *bS,
+                             const float *bP, float *rel1, float *rel2, long long ss, int P, int N2,
+                             const int *nxs, const int *rx0s, SnapBand b, int nsteps, int k, int compen,
+                             int shot0)
+{
+    const int shot = blockIdx.y + shot0;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)b.zn * b.xn) return;
+    int z, x;
+    if (!band_cell(b, i, rx0s[shot], nxs[shot], N2, z, x)) return;
+    const long long g = (long long)shot * ss + (long long)z * P + x;
+    const long long o = ((long long)shot * nsteps + k) * b.zn * b.xn + i;
+    const float sv = bS[o];
+    if (compen) rel1[g] = fmaf(racc[g], tot[g] - bP[o], rel1[g]);
+    else rel1[g] = fmaf(R[g], sv, rel1[g]);
+    rel2[g] = fmaf(sv, sv, rel2[g]);
+}
+
 // Imaging at snapshot step k of the backward run, over the interior of the
-// launch's shots (a streaming pass after the step's stencil): with the
-// stored source field S(k) and, compensated, the source's running sum
-// Tot - P_k (Tot: the forward run's total, P_k: the stored prefix) times the
-// receiver field's running sum, or, plain, the receiver field R(k) itself;
-// w is the step's share of the time sum (kernel.cu:489-517's accumulations).
+// launch's shots outside the receiver band (a streaming pass after the
+// step's stencil): with the stored source field S(k) and, compensated, the
+// source's running sum Tot - P_k (Tot: the forward run's total, P_k: the
+// stored prefix) times the receiver field's running sum, or, plain, the
+// receiver field R(k) itself; w is the step's share of the time sum
+// (kernel.cu:489-517's accumulations).
 __global__ void k_snap_image(const float *R, const float *racc, const float *tot, const void *snapS,
                              const float *snapQ, const float *scale, float *rel1, float *rel2, long long ss,
-                             int NZ, int P, int N2, const int *nxs, int nslots, int slot, int prec, int pitch,
-                             int off, float w, int compen, int shot0)
+                             int NZ, int P, int N2, const int *nxs, const int *rx0s, SnapBand b, int nslots,
+                             int slot, int prec, int pitch, int off, float w, int compen, int shot0)
 {
     const int shot = blockIdx.y + shot0;
     const int nx = nxs[shot] - 2 * N2, nz = NZ - 2 * N2;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)nz * nx) return;
     const int z = N2 + (int)(i / nx), x = N2 + (int)(i % nx);
+    if (in_band(b, z, x, rx0s[shot])) return;  // imaged at every step
     const long long g = (long long)shot * ss + (long long)z * P + x;
     const long long sl = (long long)shot * nslots + slot;
     const long long o = (sl * nz + (z - N2)) * pitch + (x - N2 + off);

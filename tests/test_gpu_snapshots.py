@@ -72,6 +72,16 @@ def test_every_step_fp32_windows_equal_ring_scheme(product_lib, cuda_ok):
     assert d_img < TOL and d_ill < TOL
 
 
+def _band_cells(p, half=24):
+    """Cells of the band imaged at every step: `half` cells on each side of
+    the receiver line, rows clipped to the interior."""
+    rz0, rx0, rdz, rdx, n = p.rec
+    zl, zh = min(rz0, rz0 + (n - 1) * rdz), max(rz0, rz0 + (n - 1) * rdz)
+    z0 = max(p.N2, zl - half)
+    zn = min(p.NZ - p.N2 - 1, zh + half) - z0 + 1
+    return zn * (abs((n - 1) * rdx) + 2 * half + 1)
+
+
 def test_snapshot_arguments_and_bytes(product_lib, cuda_ok):
     p = small_problem(M=4, N2=8, nz=40, nx=60, NT=103)
     with Engine(p, batch=3) as e:
@@ -85,10 +95,11 @@ def test_snapshot_arguments_and_bytes(product_lib, cuda_ok):
         slots = 3 + (p.NT - 5) // 4  # steps 0, 1, 2, 6, 10, .. <= NT-3
         pitch = (p.nx + p.N2 % 8 + 7) // 8 * 8
         assert got["every"] == 4 and got["precision"] == capi.RTM_RING_I16
-        assert got["bytes"] == 3 * slots * p.nz * pitch * (2 + 4)  # S in 2 bytes, its running sum in 4
+        band = 3 * (p.NT - 2) * _band_cells(p) * (4 + 4)  # the receiver band, every step, fp32
+        assert got["bytes"] == 3 * slots * p.nz * pitch * (2 + 4) + band  # S in 2 bytes, its sum in 4
         assert e.device_bytes >= base + got["bytes"]
         e.set_snapshots(2, capi.RTM_RING_F32)
-        assert e.snapshots()["bytes"] == 3 * (3 + (p.NT - 5) // 2) * p.nz * pitch * (4 + 4)
+        assert e.snapshots()["bytes"] == 3 * (3 + (p.NT - 5) // 2) * p.nz * pitch * (4 + 4) + band
         e.set_snapshots(0)
         assert e.snapshots()["bytes"] == 0 and e.device_bytes == base
 
