@@ -387,13 +387,25 @@ double snap_weight(int k, int K, int N)
     return w;
 }
 
-// The receiver band's cells of step k (k <= NT-3) of n shots.
-void band_store(rtm_ctx *c, const float *lev, int k, int qzero, int shot0, int n, cudaStream_t st)
+// The receiver band's part of the pad launches of a migration with
+// snapshots: mode 1 stores the band cells of forward step k, mode 2 images
+// them at backward step k (0: none).  Returns the extra threads per shot.
+long pad_band(rtm_ctx *c, eng::PadArgs &pa, int mode, int k)
 {
-    if (!c->band.zn) return;
-    eng::k_band_store<<<dim3(cdiv((long)c->band.zn * c->band.xn, 256), n), 256, 0, st>>>(
-        lev, c->pacc, c->ss, c->P, c->N2, c->gnx, c->grx0, c->band, c->NT - 2, k, qzero, c->bandS, c->bandP, shot0);
-    c->launches++;
+    pa.band_mode = c->band.zn ? mode : 0;
+    if (!pa.band_mode) return 0;
+    pa.band = c->band;
+    pa.band_k = k;
+    pa.band_steps = c->NT - 2;
+    pa.band_qzero = 0;
+    pa.bandS = c->bandS;
+    pa.bandP = c->bandP;
+    pa.sum = c->pacc;
+    pa.racc = c->racc;
+    pa.rel1 = c->rel1;
+    pa.rel2 = c->rel2;
+    pa.compen = c->p.compen;
+    return (long)c->band.zn * c->band.xn;
 }
 
 // Stores the snapshot of step k of n shots from the source level `lev` (its
@@ -408,7 +420,6 @@ void snap_store(rtm_ctx *c, const float *lev, int k, int qzero, int shot0, int n
                                               c->snap_nslots, slot, shot0);
         c->launches++;
     }
-    band_store(c, lev, k, qzero, shot0, n, st);
     eng::k_snap_store<<<grid, 256, 0, st>>>(lev, c->pacc, c->ss, c->NZ, c->P, c->N2, c->gnx, c->snap_amax,
                                             c->snap_scale, c->snap_nslots, slot, qzero, c->snap_prec,
                                             c->snap_pitch, c->snap_off, c->snapS, c->snapQ, shot0);
@@ -517,6 +528,11 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         RTM_CUDA_TRY(cudaMemsetAsync(c->snap_amax, 0, sizeof(unsigned) * (size_t)nb * c->snap_nslots, c->st));
         snap_store(c, c->S[0], 0, 1, 0, nb, c->st);
         snap_store(c, c->S[1], 1, 0, 0, nb, c->st);
+        if (c->band.zn) {
+            eng::k_band_start<<<dim3(cdiv((long)c->band.zn * c->band.xn, 256), nb), 256, 0, c->st>>>(
+                c->S[1], ss, c->P, c->N2, c->gnx, c->grx0, c->band, NT - 2, c->bandS, c->bandP);
+            c->launches++;
+        }
     }
     if (c->M > 0 && !snap) {
         if (r16)
@@ -561,18 +577,17 @@ int enqueue_forward(rtm_ctx *c, int nb, bool rec_on)
         }
         pa.rec = rec_on ? c->rec + (long long)(k - 1) * c->nrec : nullptr;
         pa.rec_ss = rss;
+        const long bextra = pad_band(c, pa, snap && k <= NT - 3 ? 1 : 0, k);
         for (int h = 0; h < nh; ++h) {
             sa.shot0 = pa.shot0 = hv[h].shot0;
             tic(c);
             if (int rc = launch_step(c, mode, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 0);
             tic(c);
-            launch_pad(c, pa, hv[h].n, extra, hv[h].st);
+            launch_pad(c, pa, hv[h].n, extra + bextra, hv[h].st);
             toc(c, 2);
-            if (snap && k <= NT - 3) {  // the backward run images k <= NT-3
-                if (snap_slot(k, c->snap_every) >= 0) snap_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
-                else band_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
-            }
+            if (snap && k <= NT - 3 && snap_slot(k, c->snap_every) >= 0)  // the backward run images k <= NT-3
+                snap_store(c, a2, k, 0, hv[h].shot0, hv[h].n, hv[h].st);
         }
     }
     join(c, nh);
@@ -616,7 +631,9 @@ int enqueue_backward(rtm_ctx *c, int nb)
         pa.a0 = c->R[i0]; pa.a1 = c->R[i1]; pa.a2 = c->R[i2];
         pa.ring_mode = c->M > 0 && !snap ? 2 : 0;
         if (snap) sa.pacc = c->racc;
+        const long bextra = pad_band(c, pa, snap ? 2 : 0, k);
         const float w = snap ? (float)snap_weight(k, c->snap_every, NT - 3) : 0.0f;
+
         pa.ring = c->ring ? c->ring + (long long)k * c->ringsz : nullptr;
         pa.slot = k;
         pa.s2 = c->S[i2];
@@ -626,12 +643,6 @@ int enqueue_backward(rtm_ctx *c, int nb)
             tic(c);
             if (int rc = launch_step(c, mode, sm, sa, hv[h].n, hv[h].st)) return rc;
             toc(c, 1);
-            if (snap && c->band.zn) {
-                eng::k_band_image<<<dim3(cdiv((long)c->band.zn * c->band.xn, 256), hv[h].n), 256, 0, hv[h].st>>>(
-                    c->R[i2], c->racc, c->pacc, c->bandS, c->bandP, c->rel1, c->rel2, c->ss, c->P, c->N2, c->gnx,
-                    c->grx0, c->band, NT - 2, k, c->p.compen, hv[h].shot0);
-                c->launches++;
-            }
             if (w != 0.0f) {
                 eng::k_snap_image<<<dim3(cdiv((long)c->nz * c->nx, 256), hv[h].n), 256, 0, hv[h].st>>>(
                     c->R[i2], c->racc, c->pacc, c->snapS, c->snapQ, c->snap_scale, c->rel1, c->rel2, c->ss,
@@ -640,7 +651,7 @@ int enqueue_backward(rtm_ctx *c, int nb)
                 c->launches++;
             }
             tic(c);
-            launch_pad(c, pa, hv[h].n, 0, hv[h].st);
+            launch_pad(c, pa, hv[h].n, bextra, hv[h].st);
             toc(c, 2);
         }
     }

@@ -1003,6 +1003,48 @@ __global__ void __launch_bounds__(NTHREADS, MODE == MODE_BWD ? 1 : 2)
 // Pad kernel: one-way update + blend of the absorbing pad (kernel.cu:116-183),
 // ring save / restore, receiver recording.
 
+// The band of cells around a shot's receiver line that a migration with
+// snapshots images at every step (rows z0 .. z0+zn-1 of the padded grid,
+// inside the interior; xn columns from the shot's first receiver column plus
+// xoff, clipped to its interior).  There the receiver field is held to the
+// recorded data, whose content reaches far above the sampled steps' rate.
+struct SnapBand {
+    int z0, zn, xoff, xn;
+};
+
+__device__ __forceinline__ bool in_band(const SnapBand &b, int z, int x, int rx0)
+{
+    const int xb = x - (rx0 + b.xoff);
+    return z >= b.z0 && z < b.z0 + b.zn && xb >= 0 && xb < b.xn;
+}
+
+// Band cell i of a shot: its padded-grid row and column (false: outside the
+// shot's interior).
+__device__ __forceinline__ bool band_cell(const SnapBand &b, long long i, int rx0, int NX, int N2, int &z,
+                                          int &x)
+{
+    z = b.z0 + (int)(i / b.xn);
+    x = rx0 + b.xoff + (int)(i % b.xn);
+    return x >= N2 && x < NX - N2;
+}
+
+// The receiver band's cells of the two start levels (forward run, before
+// its first step): level 0 (zero) in slot 0 and level 1 (the start-up spike)
+// in slot 1, their running sums before them being zero.
+__global__ void k_band_start(const float *S1, long long ss, int P, int N2, const int *nxs, const int *rx0s,
+                             SnapBand b, int nsteps, float *bS, float *bP)
+{
+    const int shot = blockIdx.y;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)b.zn * b.xn) return;
+    int z, x;
+    if (!band_cell(b, i, rx0s[shot], nxs[shot], N2, z, x)) return;
+    const long long o0 = (long long)shot * nsteps * b.zn * b.xn + i, o1 = o0 + (long long)b.zn * b.xn;
+    bS[o0] = 0.0f;
+    bS[o1] = S1[(long long)shot * ss + (long long)z * P + x];
+    if (bP) bP[o0] = bP[o1] = 0.0f;
+}
+
 struct PadArgs {
     int NZ, P, N2, M;
     int shot0;                // first shot of this launch (blockIdx.y + shot0)
@@ -1040,6 +1082,18 @@ struct PadArgs {
     unsigned *amax;          // [shot][NT] float bits of max |value|
     float *scale;            // [shot][NT] dequantisation factor
     int slot, qslot;         // slot written (fwd) / restored (bwd); slot to quantise (<0: none)
+    // the receiver band of a migration with source snapshots, on extra
+    // threads after the others: band_mode 1 (forward) stores the band cells
+    // of the source field of step band_k and its running sum before the step
+    // (sum: the running sum after it; band_qzero: level 0), fp32, at
+    // [shot][band_k][cell]; band_mode 2 (backward) applies the imaging
+    // condition of step band_k to them with weight 1 (sum: the forward
+    // total; racc: the receiver field's running sum; R(k): a2)
+    SnapBand band;
+    int band_mode, band_k, band_steps, band_qzero, compen;
+    float *bandS, *bandP;
+    const float *sum, *racc;
+    float *rel1, *rel2;
 };
 
 // Value a step's max |ring value| maps to: 16384 for FP16 / BF16 (FP16 keeps
@@ -1092,70 +1146,6 @@ __global__ void k_snap_store(const float *S, const float *pacc, long long ss, in
     if (prec == 0) static_cast<float *>(outS)[o] = sv;
     else static_cast<uint16_t *>(outS)[o] = ring_quant(sv, inv, prec);
     if (outQ) outQ[o] = qzero ? 0.0f : pacc[g] - sv;
-}
-
-// The band of cells around a shot's receiver line that a migration with
-// snapshots images at every step (rows z0 .. z0+zn-1 of the padded grid,
-// inside the interior; xn columns from the shot's first receiver column plus
-// xoff, clipped to its interior).  There the receiver field is held to the
-// recorded data, whose content reaches far above the sampled steps' rate.
-struct SnapBand {
-    int z0, zn, xoff, xn;
-};
-
-__device__ __forceinline__ bool in_band(const SnapBand &b, int z, int x, int rx0)
-{
-    const int xb = x - (rx0 + b.xoff);
-    return z >= b.z0 && z < b.z0 + b.zn && xb >= 0 && xb < b.xn;
-}
-
-// Band cell i of a shot: its padded-grid row and column (false: outside the
-// shot's interior).
-__device__ __forceinline__ bool band_cell(const SnapBand &b, long long i, int rx0, int NX, int N2, int &z,
-                                          int &x)
-{
-    z = b.z0 + (int)(i / b.xn);
-    x = rx0 + b.xoff + (int)(i % b.xn);
-    return x >= N2 && x < NX - N2;
-}
-
-// Forward run, every step k <= NT-3: the band cells of the source field S(k)
-// and of its running sum before the step (qzero: level 0), fp32, at
-// [shot][k][cell].
-__global__ void k_band_store(const float *S, const float *pacc, long long ss, int P, int N2, const int *nxs,
-                             const int *rx0s, SnapBand b, int nsteps, int k, int qzero, float *bS, float *bP,
-                             int shot0)
-{
-    const int shot = blockIdx.y + shot0;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)b.zn * b.xn) return;
-    int z, x;
-    if (!band_cell(b, i, rx0s[shot], nxs[shot], N2, z, x)) return;
-    const long long g = (long long)shot * ss + (long long)z * P + x;
-    const long long o = ((long long)shot * nsteps + k) * b.zn * b.xn + i;
-    const float sv = S[g];
-    bS[o] = sv;
-    if (bP) bP[o] = qzero ? 0.0f : pacc[g] - sv;
-}
-
-// Backward run, every step k: the imaging condition on the band cells, as
-// the ring scheme applies it at every step (weight 1).
-__global__ void k_band_image(const float *R, const float *racc, const float *tot, const float *bS,
-                             const float *bP, float *rel1, float *rel2, long long ss, int P, int N2,
-                             const int *nxs, const int *rx0s, SnapBand b, int nsteps, int k, int compen,
-                             int shot0)
-{
-    const int shot = blockIdx.y + shot0;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)b.zn * b.xn) return;
-    int z, x;
-    if (!band_cell(b, i, rx0s[shot], nxs[shot], N2, z, x)) return;
-    const long long g = (long long)shot * ss + (long long)z * P + x;
-    const long long o = ((long long)shot * nsteps + k) * b.zn * b.xn + i;
-    const float sv = bS[o];
-    if (compen) rel1[g] = fmaf(racc[g], tot[g] - bP[o], rel1[g]);
-    else rel1[g] = fmaf(R[g], sv, rel1[g]);
-    rel2[g] = fmaf(sv, sv, rel2[g]);
 }
 
 // Imaging at snapshot step k of the backward run, over the interior of the
@@ -1290,6 +1280,29 @@ __global__ void __launch_bounds__(256) k_pad(const PadArgs a)
             const float inv = mx > 0.0f ? tgt / mx : 0.0f;
             a.ring16[sl * a.ringsz + j] = ring_quant(a.qstage[(long long)shot * a.ringsz + j], inv, a.ring_prec);
             if (j == 0) a.scale[sl] = mx / tgt;
+            return;
+        }
+        if (a.ring_prec && a.ring_mode == 1) j -= a.ringsz;
+        if (a.band_mode) {
+            const long nb = (long)a.band.zn * a.band.xn;
+            int z, x;
+            if (j < nb) {
+                if (!band_cell(a.band, j, a.rx0s[shot], a.nxs[shot], a.N2, z, x)) return;
+                const long long g = so + (long long)z * a.P + x;
+                const long long o = ((long long)shot * a.band_steps + a.band_k) * nb + j;
+                if (a.band_mode == 1) {
+                    const float sv = a.a2[g];
+                    a.bandS[o] = sv;
+                    if (a.bandP) a.bandP[o] = a.band_qzero ? 0.0f : a.sum[g] - sv;
+                } else {
+                    const float sv = a.bandS[o];
+                    if (a.compen) a.rel1[g] = fmaf(a.racc[g], a.sum[g] - a.bandP[o], a.rel1[g]);
+                    else a.rel1[g] = fmaf(a.a2[g], sv, a.rel1[g]);
+                    a.rel2[g] = fmaf(sv, sv, a.rel2[g]);
+                }
+                return;
+            }
+            j -= nb;
         }
         return;
     }
