@@ -107,3 +107,35 @@ def test_reference_arm_runs_without_the_product_library(tmp_path):
     assert line["config"] == bench.Config(_args("--small", "--nt", "16")).workload()
     assert line["cpu_baseline"]["kind"] in ("reference", "port")
     assert "reference_gpu" in line  # timed, or "unavailable" without a GPU
+
+
+def test_snapshot_option_config_and_bytes():
+    """--snap: the config names the snapshot storage and drops the rings;
+    the snapshot bytes per shot follow the engine's layout (slots 0, 1, 2,
+    2+K, .. <= NT-3 of the interior at a pitch of 8 values, source field and
+    its running sum; the band of 24 cells around the surface receiver line at
+    every step, fp32)."""
+    cfg = bench.Config(_args("--snap", "4", "--snap-storage", "f16"))
+    w = cfg.workload()
+    assert w["snapshots"] == {"every": 4, "storage": "f16"} and w["ring_storage"] == "none"
+    assert "snapshots every 4 steps" in w["workload"]
+    slots = 3 + (cfg.NT - 5) // 4
+    pitch = (cfg.nx + cfg.N2 % 8 + 7) // 8 * 8
+    band = (1 + 24 + 1) * (cfg.nx - 1 + 2 * 24 + 1) * (cfg.NT - 2) * 8
+    assert cfg.snap_bytes() == slots * cfg.nz * pitch * (2 + 4) + band
+    assert bench.Config(_args()).workload()["snapshots"] is None
+
+
+def test_reference_arm_refuses_snapshots(capsys):
+    """The reference stores no snapshots: its arm prints its unavailable line
+    (and exits 0) instead of timing a different migration."""
+    old = sys.argv
+    sys.argv = ["bench.py", "--impl", "reference", "--snap", "4"]
+    try:
+        bench.main()
+    finally:
+        sys.argv = old
+    line = capsys.readouterr().out.strip().splitlines()[-1]
+    import json
+    d = json.loads(line)
+    assert d["impl"] == "reference" and "snapshots" in d["unavailable"]
