@@ -804,9 +804,7 @@ def run_multishot(a, cfg):
         from rtm_gpu_gb300.shard import shard_shots
         survey = synth.surface_shots(cfg.nx, nshot * world, cfg.N2)
         shots = [survey[i] for i in shard_shots(len(survey), rank, world)]
-    # with snapshots, 32 shots per batch (their snapshots, 2 GB per shot
-    # here, and the receiver band's every-step copies fit the device)
-    batch = a.batch or (min(nshot, 32) if cfg.snap else nshot)
+    batch = a.batch or nshot
     src = [pmig.src_flat(z, x) for z, x in shots]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
