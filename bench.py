@@ -108,7 +108,12 @@ def parse():
                     help="c1: the single-shot 201x401 configuration; rvsp: batched uneven "
                          "aperture windows, well receivers, autotuned; c5: learned coefficients, "
                          "1201x4001 model, FP16 rings, uneven apertures")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.snap and a.workload != "multishot":
+        ap.error("--snap applies to the multishot workload")
+    if a.snap < 0:
+        ap.error("--snap takes a positive step count")
+    return a
 
 
 class Config:

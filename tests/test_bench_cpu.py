@@ -139,3 +139,10 @@ def test_reference_arm_refuses_snapshots(capsys):
     import json
     d = json.loads(line)
     assert d["impl"] == "reference" and "snapshots" in d["unavailable"]
+
+
+@pytest.mark.parametrize("argv", [["--snap", "4", "--workload", "c1"], ["--snap", "4", "--workload", "rvsp"],
+                                  ["--snap", "-1"]])
+def test_snapshot_option_only_where_it_applies(argv):
+    with pytest.raises(SystemExit):
+        _args(*argv)
