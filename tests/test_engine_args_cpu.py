@@ -61,3 +61,12 @@ def test_null_arguments(product_lib):
     assert capi.lib().rtm_ctx_create(None, None, 1, None) == -1
     assert capi.lib().rtm_ctx_autotune(None, 1, None, None, None, 10, None) == -1
     assert capi.lib().rtm_ctx_set_kernel(None, 0, 0, 0) == -1
+
+
+def test_snapshot_calls_need_a_context(product_lib):
+    """rtm_ctx_set_snapshots / rtm_ctx_get_snapshots reject a null context
+    before any device work."""
+    lib = capi.lib()
+    assert lib.rtm_ctx_set_snapshots(None, 4, capi.RTM_RING_F16) == capi.RTM_ERR_ARG
+    e, p, b = C.c_int(), C.c_int(), C.c_size_t()
+    assert lib.rtm_ctx_get_snapshots(None, C.byref(e), C.byref(p), C.byref(b)) == capi.RTM_ERR_ARG
